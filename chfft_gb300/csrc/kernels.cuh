@@ -1,0 +1,73 @@
+// Kernel argument block and host-callable launchers shared by the kernel
+// translation units and the host plan code.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "engine.cuh"
+
+namespace chfft {
+
+// One argument block for every transform kernel. Fields a kernel does not
+// use stay zero. Element counts are in complex elements unless noted.
+struct KArgs {
+  CoreDesc core;           // complex core FFT (mixed radix or Bluestein)
+  int tpb;                 // sequences (or columns) per CTA
+  int ld;                  // shared-memory stride per sequence
+  int back;                // 1: backward transform (conjugation trick)
+  long long count;         // transforms in the batch
+  long long tiles_per_tr;  // CTAs per transform (column kernels)
+  const void* in;
+  void* out;
+  double scale;            // user scale factor (rounded to the working dtype)
+  long long in_dist;       // elements between consecutive transforms (input)
+  long long out_dist;      // elements between consecutive transforms (output)
+  int ncols;               // column kernels: row length (distance between rows)
+  int n_user;              // real transform length (MDCT)
+  const void* aux0;        // kind tables (coef, twiddle)
+  const void* aux1;        // second table (omega_4N, window)
+  double aux_scalar;       // kind constant (DCT ortho factor)
+  int* err;                // device error word, may be null
+};
+
+enum class Kernel : int {
+  C2C = 0,
+  COLS = 1,
+  R2C = 2,
+  C2R = 3,
+  DCT2 = 4,
+  DCT3 = 5,
+  MDCT = 6,
+  IMDCT = 7,
+};
+
+// Launch `which` for dtype T (float or double) with `blocks` CTAs of
+// `threads` threads and `smem` bytes of dynamic shared memory; `blue`
+// selects the Bluestein core.
+template <typename T>
+cudaError_t launch_kernel(Kernel which, bool blue, const KArgs& a, unsigned blocks, unsigned threads, size_t smem,
+                          cudaStream_t stream);
+
+// Table generators (FP64 arithmetic, stored in the working dtype T).
+enum class Table : int {
+  OMEGA = 0,       // out[k] = exp(-2 pi i k / n), k < count
+  CHIRP = 1,       // out[k] = exp(-pi i (k*k mod 2n) / n), k < count
+  RCOEF = 2,       // out[k] = (1 + i omega_n^k) / 2
+  RBCOEF = 3,      // out[k] = (1 - i omega_n^-k) / 2
+  OMEGA4N_POS = 4, // out[k] = exp(+2 pi i k / (4n))
+  OMEGA4N_NEG = 5, // out[k] = exp(-2 pi i k / (4n))
+  MDCT_TW = 6,     // out[k] = exp(-2 pi i (8k+1) / (8n)) * (2/n)^(1/4)
+  SINE_WIN = 7,    // real: sin(pi (k + 1/2) / n)
+  VORBIS_WIN = 8,  // real: sin(pi/2 sin^2(pi (k + 1/2) / n))
+  BLUE_B = 9,      // f64 only: Bluestein kernel sequence for user length n, padded length m, x 1/m
+  CHIRP_INDEX = 10 // u64: k*k mod 2n
+};
+
+template <typename T>
+cudaError_t gen_table(Table which, long long n, long long count, long long m, void* out, cudaStream_t stream);
+
+// Elementwise f64 -> T complex conversion (Bluestein spectrum rounding).
+template <typename T>
+cudaError_t convert_from_f64(const double2* src, void* dst, long long count, cudaStream_t stream);
+
+}  // namespace chfft

@@ -1,0 +1,266 @@
+// Plan compiler: radix selection, Bluestein padding and the FP64-generated
+// tables of a complex core FFT, plus launch geometry.
+//
+// chfft picks mixed radix when N is 7-smooth and Chirp-Z otherwise, with
+// M = next_pow2(N) << 1 (src/cfft1d.rs:103-206). The same split is kept;
+// the radices differ (16/8/4/2/10/5/3/7 Stockham passes instead of chfft's
+// 4/2/3/5/generic DIT stages, src/mixed_radix.rs:104-166) and M is the
+// cheapest 7-smooth length >= 2N-1, which gives the same convolution.
+#include "plan.hpp"
+
+#include <algorithm>
+#include <climits>
+
+namespace chfft {
+
+void cuda_check(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return;
+  int code = (e == cudaErrorMemoryAllocation) ? 5 /*CHFFT_ENOMEM*/ : 4 /*CHFFT_ECUDA*/;
+  throw Fail{code, std::string(what) + ": " + cudaGetErrorString(e)};
+}
+
+void DevBuf::release() {
+  if (p) cudaFree(p);
+  p = nullptr;
+  bytes = 0;
+}
+
+void DevBuf::ensure(size_t b) {
+  if (b <= bytes && p) return;
+  release();
+  if (b == 0) return;
+  CHFFT_CUDA(cudaMalloc(&p, b));
+  bytes = b;
+}
+
+Smooth factor_smooth(long long n) {
+  Smooth s;
+  if (n <= 0) return s;
+  while (n % 2 == 0) n /= 2, s.e2++;
+  while (n % 3 == 0) n /= 3, s.e3++;
+  while (n % 5 == 0) n /= 5, s.e5++;
+  while (n % 7 == 0) n /= 7, s.e7++;
+  s.ok = (n == 1);
+  return s;
+}
+
+static int radix_index(int r) {
+  for (int i = 0; i < kNumRadix; i++)
+    if (radix_at(i) == r) return i;
+  return -1;
+}
+
+bool make_stages(long long n, StageList* out) {
+  StageList st{};
+  st.n = (int)n;
+  Smooth s = factor_smooth(n);
+  if (!s.ok || n > INT_MAX) return false;
+  // t radix-10 passes absorb t twos and t fives; choose t for fewest passes.
+  int best_t = 0, best_passes = INT_MAX;
+  for (int t = 0; t <= std::min(s.e2, s.e5); t++) {
+    int twos = s.e2 - t;
+    int passes = s.e7 + s.e3 + (s.e5 - t) + t + (twos + 3) / 4;
+    if (passes < best_passes || (passes == best_passes && t > best_t)) {
+      best_passes = passes;
+      best_t = t;
+    }
+  }
+  int cnt[kNumRadix] = {0};
+  cnt[radix_index(10)] = best_t;
+  cnt[radix_index(5)] = s.e5 - best_t;
+  cnt[radix_index(3)] = s.e3;
+  cnt[radix_index(7)] = s.e7;
+  // Powers of two: p = ceil(twos/4) passes of near-equal size.
+  int twos = s.e2 - best_t;
+  int p2 = (twos + 3) / 4;
+  for (int i = 0; i < p2; i++) {
+    int bits = twos / p2 + (i < twos % p2 ? 1 : 0);
+    cnt[radix_index(1 << bits)]++;
+  }
+  st.npass = 0;
+  for (int i = 0; i < kNumRadix; i++) {
+    st.all[i] = cnt[i];
+    st.mid[i] = cnt[i];
+    st.npass += cnt[i];
+  }
+  st.rf = st.rl = 0;
+  if (st.npass >= 2) {
+    for (int i = 0; i < kNumRadix; i++)
+      if (st.mid[i] > 0) {
+        st.rf = radix_at(i);
+        st.mid[i]--;
+        break;
+      }
+    for (int i = kNumRadix - 1; i >= 0; i--)
+      if (st.mid[i] > 0) {
+        st.rl = radix_at(i);
+        st.mid[i]--;
+        break;
+      }
+  }
+  *out = st;
+  return true;
+}
+
+int threads_needed(const StageList& st, int ept, int tpb) {
+  long long need = 1;
+  for (int i = 0; i < kNumRadix; i++) {
+    if (st.all[i] == 0) continue;
+    int r = radix_at(i);
+    long long k = ept / r;
+    long long nb = (long long)tpb * (st.n / r);
+    need = std::max(need, (nb + k - 1) / k);
+  }
+  return (int)std::min<long long>(need, INT_MAX);
+}
+
+bool fits_cta(const StageList& st, int dtype) {
+  if (threads_needed(st, ept_of(dtype), 1) > kMaxThreads) return false;
+  return (size_t)smem_ld(st.n) * cplx_bytes(dtype) <= kMaxSmem;
+}
+
+long long bluestein_length(long long n, int dtype) {
+  long long lo = 2 * n - 1, best = -1;
+  double best_cost = 1e300;
+  long long hi = 1;
+  while (hi < lo) hi <<= 1;
+  for (long long m = lo; m <= hi; m++) {
+    StageList st;
+    if (!make_stages(m, &st) || !fits_cta(st, dtype)) continue;
+    double cost = (double)m * (st.npass + 0.5);
+    if (cost < best_cost) {
+      best_cost = cost;
+      best = m;
+    }
+  }
+  return best;
+}
+
+static void fft_f64_inplace(double2* d_data, const Core& c64, cudaStream_t s);
+
+bool Core::build(long long n_, int dtype_, cudaStream_t s) {
+  n = n_;
+  dtype = dtype_;
+  blue = false;
+  tw.release();
+  chirp.release();
+  bhat.release();
+  const size_t cb = cplx_bytes(dtype);
+  if (n == 1) {
+    st = StageList{};
+    st.n = 1;
+    return true;
+  }
+  if (make_stages(n, &st) && fits_cta(st, dtype)) {
+    tw.ensure(n * cb);
+    CHFFT_CUDA(dtype == 0 ? gen_table<float>(Table::OMEGA, n, n, 0, tw.p, s)
+                          : gen_table<double>(Table::OMEGA, n, n, 0, tw.p, s));
+    return true;
+  }
+  // Bluestein core (src/chirpz.rs): chirp table and the spectrum of the
+  // conjugate chirp, both from FP64.
+  long long m = bluestein_length(n, dtype);
+  if (m < 0) return false;
+  blue = true;
+  make_stages(m, &st);
+  tw.ensure(m * cb);
+  chirp.ensure(n * cb);
+  bhat.ensure(m * cb);
+  CHFFT_CUDA(dtype == 0 ? gen_table<float>(Table::OMEGA, m, m, 0, tw.p, s)
+                        : gen_table<double>(Table::OMEGA, m, m, 0, tw.p, s));
+  CHFFT_CUDA(dtype == 0 ? gen_table<float>(Table::CHIRP, n, n, 0, chirp.p, s)
+                        : gen_table<double>(Table::CHIRP, n, n, 0, chirp.p, s));
+  // B^ = FFT_M(b) / M in FP64 when the f64 engine can run length M in one
+  // CTA; otherwise the FFT of the FP64 sequence runs in the working dtype.
+  DevBuf b64;
+  b64.ensure(m * sizeof(double2));
+  CHFFT_CUDA(gen_table<double>(Table::BLUE_B, n, m, m, b64.p, s));
+  Core c64;
+  StageList st64;
+  if (make_stages(m, &st64) && fits_cta(st64, 1)) {
+    c64.build(m, 1, s);
+    fft_f64_inplace(static_cast<double2*>(b64.p), c64, s);
+    if (dtype == 0)
+      CHFFT_CUDA(convert_from_f64<float>(static_cast<const double2*>(b64.p), bhat.p, m, s));
+    else
+      CHFFT_CUDA(cudaMemcpyAsync(bhat.p, b64.p, m * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+  } else {
+    CHFFT_CUDA(convert_from_f64<float>(static_cast<const double2*>(b64.p), bhat.p, m, s));
+    Core cm;
+    cm.build(m, 0, s);
+    KArgs a{};
+    a.core = cm.desc();
+    Geo g = row_geo(cm, 1);
+    a.tpb = g.tpb;
+    a.ld = g.ld;
+    a.count = 1;
+    a.in = bhat.p;
+    a.out = bhat.p;
+    a.scale = 1.0;
+    a.in_dist = a.out_dist = m;
+    CHFFT_CUDA(launch_kernel<float>(Kernel::C2C, false, a, 1, g.threads, g.smem, s));
+  }
+  CHFFT_CUDA(cudaStreamSynchronize(s));  // temporaries are freed on return
+  return true;
+}
+
+CoreDesc Core::desc() const {
+  CoreDesc d{};
+  d.st = st;
+  d.tw = tw.p;
+  d.n = (int)n;
+  d.chirp = chirp.p;
+  d.bhat = bhat.p;
+  return d;
+}
+
+static void fft_f64_inplace(double2* d_data, const Core& c64, cudaStream_t s) {
+  KArgs a{};
+  a.core = c64.desc();
+  Geo g = row_geo(c64, 1);
+  a.tpb = g.tpb;
+  a.ld = g.ld;
+  a.count = 1;
+  a.in = d_data;
+  a.out = d_data;
+  a.scale = 1.0;
+  a.in_dist = a.out_dist = c64.st.n;
+  CHFFT_CUDA(launch_kernel<double>(Kernel::C2C, false, a, 1, g.threads, g.smem, s));
+}
+
+Geo row_geo(const Core& c, long long count, int target_threads) {
+  Geo g;
+  const int ept = ept_of(c.dtype);
+  const int m = c.st.n;
+  g.ld = smem_ld(m);
+  const size_t per = (size_t)g.ld * cplx_bytes(c.dtype);
+  const int t1 = std::max(1, threads_needed(c.st, ept, 1));
+  int tpb = std::max(1, target_threads / t1);
+  tpb = (int)std::min<size_t>(tpb, std::max<size_t>(1, (64 * 1024) / per));
+  tpb = (int)std::max<long long>(1, std::min<long long>(tpb, count));
+  while (tpb > 1 && threads_needed(c.st, ept, tpb) > kMaxThreads) tpb--;
+  g.tpb = tpb;
+  int th = threads_needed(c.st, ept, tpb);
+  th = std::max(32, ((th + 31) / 32) * 32);
+  g.threads = std::min(th, kMaxThreads);
+  g.smem = (size_t)tpb * per;
+  return g;
+}
+
+Geo col_geo(const Core& c, int ncols) {
+  Geo g;
+  const int ept = ept_of(c.dtype);
+  g.ld = smem_ld(c.st.n);
+  const size_t per = (size_t)g.ld * cplx_bytes(c.dtype);
+  int tpb = c.dtype == 0 ? 16 : 8;  // 128-byte row segments
+  tpb = std::min(tpb, std::max(1, ncols));
+  while (tpb > 1 && ((size_t)tpb * per > kMaxSmem || threads_needed(c.st, ept, tpb) > kMaxThreads)) tpb--;
+  g.tpb = tpb;
+  int th = threads_needed(c.st, ept, tpb);
+  th = std::max(32, ((th + 31) / 32) * 32);
+  g.threads = std::min(th, kMaxThreads);
+  g.smem = (size_t)tpb * per;
+  return g;
+}
+
+}  // namespace chfft

@@ -1,0 +1,96 @@
+// Host-side plan compiler: radix selection, Bluestein padding, table
+// generation and launch geometry for the kernels in k_*.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+
+namespace chfft {
+
+// Error carried from deep inside plan building / execution to the C ABI.
+struct Fail {
+  int code;
+  std::string msg;
+};
+
+void cuda_check(cudaError_t e, const char* what);
+#define CHFFT_CUDA(call) ::chfft::cuda_check((call), #call)
+
+// Owning device allocation.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes) {
+    o.p = nullptr;
+    o.bytes = 0;
+  }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    release();
+    p = o.p;
+    bytes = o.bytes;
+    o.p = nullptr;
+    o.bytes = 0;
+    return *this;
+  }
+  ~DevBuf() { release(); }
+  void release();
+  void ensure(size_t b);  // grow (contents not kept)
+};
+
+constexpr size_t kMaxSmem = 227 * 1024;  // dynamic shared memory per CTA on sm_103
+
+inline int ept_of(int dtype) { return dtype == 0 ? 32 : 16; }
+inline size_t cplx_bytes(int dtype) { return dtype == 0 ? 8 : 16; }
+inline size_t real_bytes(int dtype) { return dtype == 0 ? 4 : 8; }
+
+// 2^a 3^b 5^c 7^d, or ok = false.
+struct Smooth {
+  int e2 = 0, e3 = 0, e5 = 0, e7 = 0;
+  bool ok = false;
+};
+Smooth factor_smooth(long long n);
+
+// Stage list for a 7-smooth n (fewest passes; radices 16/8/4/2/10/5/3/7).
+// Returns false when n is not 7-smooth.
+bool make_stages(long long n, StageList* out);
+// Threads a CTA needs to run `tpb` sequences with these stages.
+int threads_needed(const StageList& st, int ept, int tpb);
+// Whether one sequence of these stages fits a CTA (threads and shared memory).
+bool fits_cta(const StageList& st, int dtype);
+
+// Complex core FFT of logical length n for one dtype: mixed radix when n is
+// 7-smooth and fits a CTA, otherwise Bluestein with a 7-smooth M >= 2n-1.
+struct Core {
+  long long n = 0;
+  int dtype = 0;
+  bool blue = false;
+  StageList st{};  // stages of the FFT actually run (length M for Bluestein)
+  DevBuf tw, chirp, bhat;
+  bool build(long long n, int dtype, cudaStream_t s);  // false: unsupported size
+  CoreDesc desc() const;
+  long long fft_len() const { return st.n; }
+  size_t device_bytes() const { return tw.bytes + chirp.bytes + bhat.bytes; }
+};
+
+// Launch geometry of a CTA-per-`tpb`-sequences kernel.
+struct Geo {
+  int tpb = 1, threads = 32;
+  size_t smem = 0;
+  int ld = 0;
+};
+Geo row_geo(const Core& c, long long count, int target_threads = 256);
+Geo col_geo(const Core& c, int ncols);
+
+// Smallest 7-smooth M >= lo that the CTA engine runs cheapest (M * passes).
+long long bluestein_length(long long n, int dtype);
+
+}  // namespace chfft

@@ -1,0 +1,180 @@
+/*
+ * chfft_gpu.h — C ABI of the GB300 (sm_103a) transform engine.
+ *
+ * This is the drop-in boundary below chfft's public Rust API
+ * (src/lib.rs:21-25 of chfft 0.3.4). Each plan handle stands for one of the
+ * reference's plan structs and keeps its semantics: the plan owns its
+ * tables, is not thread-safe (the Rust methods take &mut self) and CFft1D /
+ * CFft2D plans re-plan when handed a different length, as
+ * src/cfft1d.rs:216-218 and src/cfft2d.rs:336-338 do. Errors are status
+ * codes; CHFFT_EINVAL_LEN is the reference's `panic!("invalid length")`
+ * (src/rfft1d.rs:75, src/dct1d.rs:55, src/mdct1d.rs:103).
+ *
+ * Data layout: complex values are interleaved {re, im} pairs of the working
+ * dtype (num-complex's #[repr(C)] Complex<T>); 2-D arrays are row-major
+ * M x N (the Rust wrapper flattens &[Vec<Complex<T>>]).
+ *
+ * Host-pointer calls copy to the device, run, copy back and synchronise.
+ * Device-pointer calls enqueue on the given stream and return at once.
+ * There is no CPU fallback: every transform runs in this library's kernels.
+ */
+#ifndef CHFFT_GPU_H
+#define CHFFT_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CHFFT_API __attribute__((visibility("default")))
+
+typedef enum chfft_status {
+  CHFFT_OK = 0,
+  CHFFT_EINVAL_LEN = 1,    /* the reference's panic!("invalid length") */
+  CHFFT_EINVAL = 2,        /* null pointer, unknown enum value, method not offered by the type */
+  CHFFT_EUNSUPPORTED = 3,  /* size this build does not handle */
+  CHFFT_ECUDA = 4,         /* CUDA runtime error (message in chfft_last_error) */
+  CHFFT_ENOMEM = 5,        /* device allocation failed */
+  CHFFT_ETIMEOUT = 6       /* a bounded device-side wait gave up */
+} chfft_status;
+
+typedef enum chfft_dtype { CHFFT_F32 = 0, CHFFT_F64 = 1 } chfft_dtype;
+
+typedef enum chfft_kind {
+  CHFFT_KIND_CFFT1D = 0,
+  CHFFT_KIND_CFFT2D = 1,
+  CHFFT_KIND_RFFT1D = 2,
+  CHFFT_KIND_DCT1D = 3,
+  CHFFT_KIND_MDCT1D = 4
+} chfft_kind;
+
+/* The reference's method names (src/cfft1d.rs:270-455 and the same names
+ * on the other types). Each type accepts the subset it defines:
+ *   CFft1D: all 12;  CFft2D: FORWARD..BACKWARDU (no BACKWARDN, no in-place);
+ *   RFft1D: FORWARD..BACKWARDN;  Dct1D: FORWARD..FORWARDN;
+ *   Mdct1D: FORWARD, FORWARDU, BACKWARD, BACKWARDU. */
+typedef enum chfft_method {
+  CHFFT_FORWARD = 0,
+  CHFFT_FORWARD0 = 1,
+  CHFFT_FORWARDU = 2,
+  CHFFT_FORWARDN = 3,
+  CHFFT_BACKWARD = 4,
+  CHFFT_BACKWARD0 = 5,
+  CHFFT_BACKWARDU = 6,
+  CHFFT_BACKWARDN = 7,
+  CHFFT_FORWARD0I = 8,
+  CHFFT_BACKWARD0I = 9,
+  CHFFT_FORWARDUI = 10,
+  CHFFT_BACKWARDUI = 11
+} chfft_method;
+
+/* DctType::{Two, Three} (src/dct1d.rs:37-43). */
+typedef enum chfft_dct_type { CHFFT_DCT_TWO = 2, CHFFT_DCT_THREE = 3 } chfft_dct_type;
+
+/* Mdct1D windows: with_sine / with_vorbis (src/mdct1d.rs:62-75) or a
+ * caller-evaluated window table (Mdct1D::new(window_func, len),
+ * src/mdct1d.rs:101-121, calc_window :91-93: the reference evaluates window_func(len, i) for
+ * i < len at setup; the wrapper does the same and passes the values). */
+typedef enum chfft_window { CHFFT_WINDOW_SINE = 0, CHFFT_WINDOW_VORBIS = 1, CHFFT_WINDOW_CUSTOM = 2 } chfft_window;
+
+typedef struct chfft_plan_s* chfft_plan;
+
+/* ---- plan construction (one per reference constructor) ------------------ */
+
+/* CFft1D::with_len (src/cfft1d.rs:83-92); len 0 gives CFft1D::new (:68-75). */
+CHFFT_API int chfft_cfft1d_create(int dtype, size_t len, chfft_plan* out);
+/* CFft2D::with_len (src/cfft2d.rs:93-103); 0 x 0 gives CFft2D::new. */
+CHFFT_API int chfft_cfft2d_create(int dtype, size_t len_m, size_t len_n, chfft_plan* out);
+/* RFft1D::new (src/rfft1d.rs:73-90): odd len -> CHFFT_EINVAL_LEN. */
+CHFFT_API int chfft_rfft1d_create(int dtype, size_t len, chfft_plan* out);
+/* Dct1D::new (src/dct1d.rs:53-62): odd len -> CHFFT_EINVAL_LEN. */
+CHFFT_API int chfft_dct1d_create(int dtype, int dct_type, size_t len, int is_ortho, chfft_plan* out);
+/* Mdct1D::new / with_sine / with_vorbis (src/mdct1d.rs:62-121):
+ * len % 4 != 0 -> CHFFT_EINVAL_LEN. window_table (len values of the working
+ * dtype, host memory) is read only for CHFFT_WINDOW_CUSTOM. */
+CHFFT_API int chfft_mdct1d_create(int dtype, size_t len, int window, const void* window_table, chfft_plan* out);
+CHFFT_API int chfft_plan_destroy(chfft_plan plan);
+
+/* ---- re-plan (the reference's setup methods) ---------------------------- */
+
+/* CFft1D::setup (src/cfft1d.rs:103), RFft1D::setup (src/rfft1d.rs:101),
+ * Mdct1D::setup (src/mdct1d.rs:126; a custom window must be re-supplied
+ * through window_table, NULL keeps sine/vorbis). */
+CHFFT_API int chfft_plan_setup(chfft_plan plan, size_t len, const void* window_table);
+/* CFft2D::setup (src/cfft2d.rs:114-124). */
+CHFFT_API int chfft_cfft2d_setup(chfft_plan plan, size_t len_m, size_t len_n);
+/* Dct1D::setup (src/dct1d.rs:74-86). */
+CHFFT_API int chfft_dct1d_setup(chfft_plan plan, int dct_type, size_t len, int is_ortho);
+
+/* ---- execution ---------------------------------------------------------- */
+
+/* One transform on host memory: the reference call `plan.method(&src)`.
+ * src_len / dst_len count elements of the method's input / output type
+ * (complex for complex sides, reals for real sides). For CFft1D a src_len
+ * different from the plan's length re-plans; for the in-place methods src
+ * and dst may be the same buffer. RFft1D / Dct1D / Mdct1D reject a length
+ * mismatch with CHFFT_EINVAL_LEN. dst_len must equal the output length. */
+CHFFT_API int chfft_execute(chfft_plan plan, int method, const void* src, size_t src_len, void* dst,
+                            size_t dst_len);
+/* CFft2D::method(&rows) on a row-major len_m x len_n host array (re-plans
+ * when the shape differs from the plan's). */
+CHFFT_API int chfft_execute_2d(chfft_plan plan, int method, const void* src, size_t len_m, size_t len_n,
+                               void* dst);
+/* `batch` independent transforms on host memory, each laid out back to back
+ * (input and output strides are the per-transform element counts). */
+CHFFT_API int chfft_execute_batch(chfft_plan plan, int method, const void* src, void* dst, size_t batch);
+/* `batch` transforms on device memory, enqueued on `stream` (a cudaStream_t,
+ * NULL for the legacy default stream). d_src == d_dst is allowed for
+ * complex-to-complex kinds. */
+CHFFT_API int chfft_execute_device(chfft_plan plan, int method, const void* d_src, void* d_dst, size_t batch,
+                                   void* stream);
+
+/* ---- plan inspection ---------------------------------------------------- */
+
+typedef struct chfft_plan_info {
+  int kind, dtype;
+  size_t len, len_m, len_n;  /* user lengths */
+  size_t fft_len;            /* length of the complex core FFT */
+  int algorithm;             /* 0 mixed radix in shared memory, 1 fused Bluestein, 2 four-step, 3 four-step Bluestein */
+  size_t padded_len;         /* Bluestein convolution length M (0 otherwise) */
+  int npass;                 /* radix passes of the core FFT */
+  int radix[24];
+  int seq_per_cta, threads_per_cta;
+  size_t smem_per_cta;
+  size_t in_elems, out_elems; /* per transform, in the method's element type (forward direction) */
+  size_t device_bytes;        /* tables + workspace held by the plan */
+} chfft_plan_info;
+
+CHFFT_API int chfft_plan_get_info(chfft_plan plan, chfft_plan_info* info);
+
+/* ---- index arithmetic (bit-exact with the reference's plan code) -------- */
+
+/* prime_factorization(len, max) (src/prime_factorization.rs:66-113):
+ * writes up to cap (value, count) pairs, returns the number of factors
+ * (0 when a prime exceeds max_prime; the reference's Chirp-Z trigger). */
+CHFFT_API int chfft_factorize(size_t len, size_t max_prime, size_t* values, size_t* counts, size_t cap);
+/* calc_bitreverse (src/precompute_utils.rs:70-91) for an explicit factor list;
+ * writes prod(value^count) entries. */
+CHFFT_API int chfft_digit_reversal(const size_t* values, const size_t* counts, size_t nfactors, size_t* out,
+                                   size_t out_cap);
+/* calc_bitreverse2inplace (src/precompute_utils.rs:93-104), in O(n). */
+CHFFT_API int chfft_swap_list(const size_t* gather, size_t n, size_t* out);
+/* Chirp-Z table indices (i*i) % 2N for i < len (src/cfft1d.rs:123-128),
+ * computed by a GPU kernel into device memory d_out (len uint64 values). */
+CHFFT_API int chfft_chirp_index_device(size_t len, uint64_t* d_out, void* stream);
+
+/* ---- diagnostics -------------------------------------------------------- */
+
+/* Message of the last failure on the calling thread ("" if none). */
+CHFFT_API const char* chfft_last_error(void);
+CHFFT_API const char* chfft_status_string(int status);
+/* Library version string. */
+CHFFT_API const char* chfft_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CHFFT_GPU_H */
