@@ -1,0 +1,356 @@
+#!/usr/bin/env python3
+"""Benchmark: batched FFT GFLOP/s (5 N log2 N) on the mixed-radix + Bluestein
+f32 workload, and HBM GB/s with its roofline fraction.
+
+Workload ("step" = one forward pass over the batch, all f32):
+  - CFft1D 4096 x N=1000  (2^3 5^3, mixed radix), complex N(0,1)
+  - CFft1D 4096 x N=1009  (prime, Bluestein / Chirp-Z), complex N(0,1)
+  - CFft2D 2048 x 2048,   complex uniform[-1, 1)
+Inputs are seeded synthetic data (the reference has no dataset); they sit in
+HBM before the timed region. Each timed step is bracketed by CUDA events on
+the launch stream and the L2 is flushed (256 MiB memset) between steps,
+outside the events. `e2e` runs the same workload through the C ABI's
+host-pointer entry point (chfft_execute_batch) from pinned host memory, so
+every step includes the H2D copy of the inputs and the D2H copy of the
+outputs.
+
+`--impl reference` times the CPU oracle (a C++ restatement of chfft's
+algorithm; the Rust crate cannot be built here) on the same workload with
+every host thread: one plan per thread over each 1-D batch, the 2-D
+transform on one thread as chfft's CFft2D runs.
+
+Multi-GPU: every rank runs the workload on its own GPU (independent
+replicas, no collective); value = all ranks' work / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "batched FFT GFLOP/s (5N log2N), HBM GB/s; TC vs FP32 path at fixed rel-L2"
+WORKLOAD = "cfft1d f32 4096x1000 + cfft1d f32 4096x1009 (chirp-z) + cfft2d f32 2048x2048, forward"
+PARTS = [
+    # name, kind, shape, batch, seed, distribution
+    ("c2c_1000", "cfft1d", (1000,), 4096, 2, "normal"),
+    ("c2c_1009", "cfft1d", (1009,), 4096, 2, "normal"),
+    ("c2c2d_2048", "cfft2d", (2048, 2048), 1, 3, "uniform"),
+]
+CPLX_BYTES = 8  # complex f32
+FLUSH_BYTES = 256 << 20
+
+
+def part_elems(shape):
+    return int(np.prod(shape))
+
+
+def part_flops(shape, batch):
+    n = part_elems(shape)
+    return 5.0 * n * math.log2(n) * batch
+
+
+def part_bytes(shape, batch):
+    return 2.0 * part_elems(shape) * batch * CPLX_BYTES  # one read + one write
+
+
+TOTAL_FLOPS = sum(part_flops(s, b) for _, _, s, b, _, _ in PARTS)
+TOTAL_BYTES = sum(part_bytes(s, b) for _, _, s, b, _, _ in PARTS)
+
+
+def make_input(shape, batch, seed, dist):
+    rng = np.random.default_rng(seed)
+    full = (batch,) + tuple(shape)
+    if dist == "normal":
+        x = rng.standard_normal(full, dtype=np.float32) + 1j * rng.standard_normal(full, dtype=np.float32)
+    else:
+        x = rng.uniform(-1, 1, full).astype(np.float32) + 1j * rng.uniform(-1, 1, full).astype(np.float32)
+    return x.astype(np.complex64)
+
+
+# ---------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clock / throttle samples every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.t0 = self.t1 = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        time.sleep(0.25)
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=5)
+        rows = []
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), f[5], f[6], f[7], f[8]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[2 + i].lower().startswith("active")})
+        busy = [r[0] for r in rows if r[0] >= 0.5 * r[1]] or [r[0] for r in rows]
+        return {"sm_mhz": statistics.median(busy), "sm_max_mhz": max(r[1] for r in rows), "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------- traffic
+def profiled_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "bench_dram_traffic.txt")
+    if not os.path.exists(path):
+        return {}
+    out = {}
+    for line in open(path):
+        line = line.strip()
+        if not line or line.startswith("#") or ":" not in line:
+            continue
+        k, v = line.split(":", 1)
+        try:
+            out[k.strip()] = float(v.split()[0])
+        except (ValueError, IndexError):
+            pass
+    return out
+
+
+# ---------------------------------------------------------------------------- CPU
+def cpu_run(steps: int, warmup: int, threads: int):
+    """The oracle (chfft's algorithm, C++) on the full workload; seconds per step."""
+    import oracle
+
+    inputs = [make_input(s, b, seed, d) for _, _, s, b, seed, d in PARTS]
+    per_step = []
+    for it in range(warmup + steps):
+        t = 0.0
+        for (name, kind, shape, batch, _, _), x in zip(PARTS, inputs):
+            if kind == "cfft1d":
+                _, secs = oracle.cfft1d(x, "forward", nthreads=threads, timing=True)
+            else:
+                _, secs = oracle.cfft2d(x, "forward", nthreads=1, timing=True)
+            t += secs
+        if it >= warmup:
+            per_step.append(t)
+    return per_step
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    per_step = cpu_run(args.steps, args.warmup, threads)
+    t = statistics.median(per_step)
+    v = TOTAL_FLOPS / t / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": "GFLOP/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": round(v, 3), "unit": "GFLOP/s", "cores": threads, "kind": "port",
+                         "sample": "full workload per step; 1-D batches split over all host threads (one plan "
+                                   "per thread), CFft2D on one thread"},
+        "e2e": {"value": round(v, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "hbm_gbs": round(TOTAL_BYTES / t / 1e9, 3),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------- GPU
+def run_gpu(args, rank, world, local_rank):
+    import torch
+
+    import chfft_gb300 as cg
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+
+    plans, d_in, d_out, h_in, h_out = [], [], [], [], []
+    for name, kind, shape, batch, seed, dist in PARTS:
+        x = make_input(shape, batch, seed, dist)
+        if kind == "cfft1d":
+            p = cg.CFft1D.with_len(shape[0], np.float32)
+        else:
+            p = cg.CFft2D.with_len(shape[0], shape[1], np.float32)
+        plans.append(p)
+        t_in = torch.from_numpy(x.view(np.float32)).to(dev)
+        d_in.append(t_in)
+        d_out.append(torch.empty_like(t_in))
+        hi = torch.from_numpy(x.view(np.float32).reshape(batch, -1)).pin_memory()
+        h_in.append(hi)
+        h_out.append(torch.empty_like(hi).pin_memory())
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def step(events=None):
+        for i, (p, (_, _, _, batch, _, _)) in enumerate(zip(plans, PARTS)):
+            if events is not None:
+                events[i].record(stream)
+            p.execute_device("forward", d_in[i].data_ptr(), d_out[i].data_ptr(), batch, sptr)
+        if events is not None:
+            events[len(plans)].record(stream)
+
+    # correctness guard on the measured buffers (one spot check per part)
+    step()
+    torch.cuda.synchronize()
+    for i, (name, kind, shape, batch, seed, dist) in enumerate(PARTS):
+        x = make_input(shape, batch, seed, dist)
+        y = d_out[i].cpu().numpy().view(np.complex64).reshape((batch,) + tuple(shape))
+        ref = np.fft.fftn(x[0].astype(np.complex128))
+        err = np.linalg.norm(y[0] - ref) / np.linalg.norm(ref)
+        if err > 1e-5:
+            raise SystemExit(f"{name}: rel-L2 {err:.2e} against numpy FP64; refusing to time a wrong result")
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local_rank).start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(len(plans) + 1)] for _ in range(args.steps)]
+    for k in range(args.steps):
+        flush.zero_()
+        step(ev[k])
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    part_ms = [[ev[k][i].elapsed_time(ev[k][i + 1]) for k in range(args.steps)] for i in range(len(plans))]
+    step_ms = [sum(part_ms[i][k] for i in range(len(plans))) for k in range(args.steps)]
+    ms = statistics.mean(step_ms)
+
+    # end to end through the C ABI from pinned host memory
+    def e2e_step():
+        for i, (p, (_, _, _, batch, _, _)) in enumerate(zip(plans, PARTS)):
+            p_h = p.handle
+            rc = cg.lib().chfft_execute_batch(p_h, cg.METHODS["forward"], h_in[i].data_ptr(), h_out[i].data_ptr(),
+                                              batch)
+            if rc != 0:
+                raise SystemExit(f"chfft_execute_batch failed: {cg.lib().chfft_last_error().decode()}")
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    e2e_times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_times.append(time.perf_counter() - t0)
+    clk = clocks.stop()
+    e2e_s = statistics.mean(e2e_times)
+
+    if world > 1:
+        t = torch.tensor([ms, e2e_s], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms, e2e_s = float(t[0]), float(t[1])
+    if rank != 0:
+        return 0
+
+    # dominant launch: the part with the largest mean time (one kernel each
+    # for the 1-D parts; the 2-D part is a row kernel plus a column kernel)
+    means = [statistics.mean(pm) for pm in part_ms]
+    dom = int(np.argmax(means))
+    dname, dkind, dshape, dbatch, _, _ = PARTS[dom]
+    dom_launches = 2 if dkind == "cfft2d" else 1
+    dom_ms = means[dom] / dom_launches
+    dom_bytes = part_bytes(dshape, dbatch) / dom_launches
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured"
+    if not peak:
+        peak, peak_src = 6800.0, "fallback"
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    traffic = profiled_traffic().get(dname)
+    h2d = sum(int(h.numel() * 4) for h in h_in)
+    d2h = sum(int(h.numel() * 4) for h in h_out)
+    value = world * TOTAL_FLOPS / (ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded normal / uniform)",
+        "config": {"workload": WORKLOAD, "l2": "flushed between timed steps (256 MiB memset, outside the events)",
+                   "parallelism": f"replicas x{world}"},
+        "hbm_gbs": round(world * TOTAL_BYTES / (ms * 1e-3) / 1e9, 1),
+        "parts_ms": {PARTS[i][0]: round(means[i], 4) for i in range(len(PARTS))},
+        "roofline": {"bound": "hbm", "kernel": dname, "achieved": round(achieved, 1), "peak": peak,
+                     "peak_source": f"{peak_src} hbm_gbs", "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": traffic, "algorithmic_bytes": dom_bytes},
+        "e2e": {"value": round(world * TOTAL_FLOPS / e2e_s / 1e9, 2), "unit": "GFLOP/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_s * 1e3, 3)},
+        "gpu_launches": 4 * args.steps,
+        "clocks": clk,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        per = cpu_run(steps=3, warmup=1, threads=threads)
+        t = statistics.median(per)
+        line["cpu_baseline"] = {"value": round(TOTAL_FLOPS / t / 1e9, 3), "unit": "GFLOP/s", "cores": threads,
+                                "kind": "port",
+                                "sample": "the full workload, 3 timed steps after 1 warm-up; 1-D batches over all "
+                                          "host threads, CFft2D on one thread"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    if world > 1:
+        import torch
+
+        torch.distributed.init_process_group("nccl")
+    try:
+        return run_gpu(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch
+
+            torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

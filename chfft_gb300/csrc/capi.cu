@@ -212,7 +212,7 @@ struct PlanImpl {
     a.ld = g.ld;
     a.count = count;
     unsigned blocks = (unsigned)((count + g.tpb - 1) / g.tpb);
-    CHFFT_CUDA(launch_kernel<T>(k, c.blue, a, blocks, g.threads, g.smem, s));
+    CHFFT_CUDA(launch_kernel<T>(k, c.blue, g.k1, a, blocks, g.threads, g.smem, s));
   }
 
   template <typename T>
@@ -253,7 +253,8 @@ struct PlanImpl {
         b.scale = sc;
         b.in_dist = b.out_dist = len_m * len_n;
         b.ncols = (int)len_n;
-        CHFFT_CUDA(launch_kernel<T>(Kernel::COLS, core2.blue, b, (unsigned)(batch * b.tiles_per_tr), g.threads, g.smem, s));
+        CHFFT_CUDA(launch_kernel<T>(Kernel::COLS, core2.blue, g.k1, b, (unsigned)(batch * b.tiles_per_tr), g.threads,
+                                    g.smem, s));
         return;
       }
       case CHFFT_KIND_RFFT1D:

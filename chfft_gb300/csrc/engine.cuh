@@ -37,7 +37,10 @@ CHFFT_HD constexpr int radix_at(int i) {
 
 // Complex elements one thread holds during a pass: 32 (64 registers) for
 // f32, 16 (64 registers) for f64. A pass of radix R gives each thread up to
-// EPT/R butterflies.
+// EPT/R butterflies. The K1 variants give every thread exactly one
+// butterfly per pass (R elements): smaller code, fewer registers and more
+// resident warps, usable when no pass has more than kMaxThreads butterflies
+// per CTA.
 template <typename C> struct Ept;
 template <> struct Ept<float2> { static constexpr int value = 32; };
 template <> struct Ept<double2> { static constexpr int value = 16; };
@@ -82,10 +85,10 @@ __device__ __forceinline__ void split_index(int b, int tpb, int nb, int& t, int&
 // One radix-R Stockham pass: ld -> registers -> butterflies -> st. Ns is the
 // product of the radices of the passes already run. All loads of the pass
 // complete (barrier) before any store, so ld and st may be the same tile.
-template <int R, bool TMINOR, typename C, class Ld, class St>
+template <int R, bool TMINOR, bool K1, typename C, class Ld, class St>
 __device__ __forceinline__ void pass_body(int n, int Ns, int tpb, const C* __restrict__ tw, const Ld& ld,
                                           const St& st) {
-  constexpr int K = Ept<C>::value / R;
+  constexpr int K = K1 ? 1 : Ept<C>::value / R;
   const int nb = n / R;
   const int total = tpb * nb;
   const int tw_step = (Ns > 1) ? n / (Ns * R) : 0;
@@ -126,33 +129,33 @@ __device__ __forceinline__ void pass_body(int n, int Ns, int tpb, const C* __res
 }
 
 // A single pass of runtime radix R (only ever called outside loops).
-template <bool TMINOR, typename C, class Ld, class St>
+template <bool TMINOR, bool K1, typename C, class Ld, class St>
 __device__ __forceinline__ void pass_any(int R, int n, int Ns, int tpb, const C* tw, const Ld& ld, const St& st) {
   switch (R) {
-    case 16: pass_body<16, TMINOR>(n, Ns, tpb, tw, ld, st); break;
-    case 8: pass_body<8, TMINOR>(n, Ns, tpb, tw, ld, st); break;
-    case 4: pass_body<4, TMINOR>(n, Ns, tpb, tw, ld, st); break;
-    case 2: pass_body<2, TMINOR>(n, Ns, tpb, tw, ld, st); break;
-    case 10: pass_body<10, TMINOR>(n, Ns, tpb, tw, ld, st); break;
-    case 5: pass_body<5, TMINOR>(n, Ns, tpb, tw, ld, st); break;
-    case 3: pass_body<3, TMINOR>(n, Ns, tpb, tw, ld, st); break;
-    case 7: pass_body<7, TMINOR>(n, Ns, tpb, tw, ld, st); break;
+    case 16: pass_body<16, TMINOR, K1>(n,Ns, tpb, tw, ld, st); break;
+    case 8: pass_body<8, TMINOR, K1>(n,Ns, tpb, tw, ld, st); break;
+    case 4: pass_body<4, TMINOR, K1>(n,Ns, tpb, tw, ld, st); break;
+    case 2: pass_body<2, TMINOR, K1>(n,Ns, tpb, tw, ld, st); break;
+    case 10: pass_body<10, TMINOR, K1>(n,Ns, tpb, tw, ld, st); break;
+    case 5: pass_body<5, TMINOR, K1>(n,Ns, tpb, tw, ld, st); break;
+    case 3: pass_body<3, TMINOR, K1>(n,Ns, tpb, tw, ld, st); break;
+    case 7: pass_body<7, TMINOR, K1>(n,Ns, tpb, tw, ld, st); break;
     default: break;
   }
 }
 
 // cnt[i] passes of radix radix_at(i) on the tile, in canonical order.
 // Returns the updated radix product Ns.
-template <bool TMINOR, typename C>
+template <bool TMINOR, bool K1, typename C>
 __device__ __forceinline__ int smem_passes(const int* cnt, int n, int Ns, int tpb, const C* tw, const SmemIO<C>& sm) {
-  for (int c = 0; c < cnt[0]; c++, Ns *= 16) pass_body<16, TMINOR>(n, Ns, tpb, tw, sm, sm);
-  for (int c = 0; c < cnt[1]; c++, Ns *= 8) pass_body<8, TMINOR>(n, Ns, tpb, tw, sm, sm);
-  for (int c = 0; c < cnt[2]; c++, Ns *= 4) pass_body<4, TMINOR>(n, Ns, tpb, tw, sm, sm);
-  for (int c = 0; c < cnt[3]; c++, Ns *= 2) pass_body<2, TMINOR>(n, Ns, tpb, tw, sm, sm);
-  for (int c = 0; c < cnt[4]; c++, Ns *= 10) pass_body<10, TMINOR>(n, Ns, tpb, tw, sm, sm);
-  for (int c = 0; c < cnt[5]; c++, Ns *= 5) pass_body<5, TMINOR>(n, Ns, tpb, tw, sm, sm);
-  for (int c = 0; c < cnt[6]; c++, Ns *= 3) pass_body<3, TMINOR>(n, Ns, tpb, tw, sm, sm);
-  for (int c = 0; c < cnt[7]; c++, Ns *= 7) pass_body<7, TMINOR>(n, Ns, tpb, tw, sm, sm);
+  for (int c = 0; c < cnt[0]; c++, Ns *= 16) pass_body<16, TMINOR, K1>(n,Ns, tpb, tw, sm, sm);
+  for (int c = 0; c < cnt[1]; c++, Ns *= 8) pass_body<8, TMINOR, K1>(n,Ns, tpb, tw, sm, sm);
+  for (int c = 0; c < cnt[2]; c++, Ns *= 4) pass_body<4, TMINOR, K1>(n,Ns, tpb, tw, sm, sm);
+  for (int c = 0; c < cnt[3]; c++, Ns *= 2) pass_body<2, TMINOR, K1>(n,Ns, tpb, tw, sm, sm);
+  for (int c = 0; c < cnt[4]; c++, Ns *= 10) pass_body<10, TMINOR, K1>(n,Ns, tpb, tw, sm, sm);
+  for (int c = 0; c < cnt[5]; c++, Ns *= 5) pass_body<5, TMINOR, K1>(n,Ns, tpb, tw, sm, sm);
+  for (int c = 0; c < cnt[6]; c++, Ns *= 3) pass_body<3, TMINOR, K1>(n,Ns, tpb, tw, sm, sm);
+  for (int c = 0; c < cnt[7]; c++, Ns *= 7) pass_body<7, TMINOR, K1>(n,Ns, tpb, tw, sm, sm);
   return Ns;
 }
 
@@ -233,7 +236,7 @@ __device__ __forceinline__ void spectrum_phase(const SmemIO<C>& sm, int m, int t
 // pass and the storer into the last (when the stage list has >= 2 passes);
 // otherwise they run as phases, and a loader or storer that is the tile
 // itself runs no phase.
-template <bool BLUE, bool TMINOR, bool FUSED, typename C, class Ld, class St>
+template <bool BLUE, bool TMINOR, bool FUSED, bool K1, typename C, class Ld, class St>
 __device__ __forceinline__ void core_fft(const CoreDesc& d, int tpb, const SmemIO<C>& sm, const Ld& ld,
                                          const St& st) {
   const C* tw = static_cast<const C*>(d.tw);
@@ -243,12 +246,12 @@ __device__ __forceinline__ void core_fft(const CoreDesc& d, int tpb, const SmemI
     constexpr bool kLoad = !std::is_same<Ld, SmemIO<C>>::value;
     constexpr bool kStore = !std::is_same<St, SmemIO<C>>::value;
     if (FUSED && kLoad && kStore && sg.npass >= 2) {
-      pass_any<TMINOR>(sg.rf, m, 1, tpb, tw, ld, sm);
-      const int Ns = smem_passes<TMINOR>(sg.mid, m, sg.rf, tpb, tw, sm);
-      pass_any<TMINOR>(sg.rl, m, Ns, tpb, tw, sm, st);
+      pass_any<TMINOR, K1>(sg.rf, m, 1, tpb, tw, ld, sm);
+      const int Ns = smem_passes<TMINOR, K1>(sg.mid, m, sg.rf, tpb, tw, sm);
+      pass_any<TMINOR, K1>(sg.rl, m, Ns, tpb, tw, sm, st);
     } else {
       if (kLoad) load_phase<TMINOR>(sm, m, tpb, ld);
-      smem_passes<TMINOR>(sg.all, m, 1, tpb, tw, sm);
+      smem_passes<TMINOR, K1>(sg.all, m, 1, tpb, tw, sm);
       if (kStore) store_phase<TMINOR>(sm, m, tpb, st);
     }
   } else {
@@ -260,19 +263,19 @@ __device__ __forceinline__ void core_fft(const CoreDesc& d, int tpb, const SmemI
       int cnt[kNumRadix];
 #pragma unroll
       for (int i = 0; i < kNumRadix; i++) cnt[i] = sg.mid[i] + (radix_at(i) == sg.rl ? 1 : 0);
-      pass_any<TMINOR>(sg.rf, m, 1, tpb, tw, l1, sm);
-      smem_passes<TMINOR>(cnt, m, sg.rf, tpb, tw, sm);
+      pass_any<TMINOR, K1>(sg.rf, m, 1, tpb, tw, l1, sm);
+      smem_passes<TMINOR, K1>(cnt, m, sg.rf, tpb, tw, sm);
       spectrum_phase<TMINOR>(sm, m, tpb, static_cast<const C*>(d.bhat));
       // FFT 2: every pass but rl, then rl fused with the chirp store.
 #pragma unroll
       for (int i = 0; i < kNumRadix; i++) cnt[i] = sg.mid[i] + (radix_at(i) == sg.rf ? 1 : 0);
-      const int Ns = smem_passes<TMINOR>(cnt, m, 1, tpb, tw, sm);
-      pass_any<TMINOR>(sg.rl, m, Ns, tpb, tw, sm, s2);
+      const int Ns = smem_passes<TMINOR, K1>(cnt, m, 1, tpb, tw, sm);
+      pass_any<TMINOR, K1>(sg.rl, m, Ns, tpb, tw, sm, s2);
     } else {
       load_phase<TMINOR>(sm, m, tpb, l1);
-      smem_passes<TMINOR>(sg.all, m, 1, tpb, tw, sm);
+      smem_passes<TMINOR, K1>(sg.all, m, 1, tpb, tw, sm);
       spectrum_phase<TMINOR>(sm, m, tpb, static_cast<const C*>(d.bhat));
-      smem_passes<TMINOR>(sg.all, m, 1, tpb, tw, sm);
+      smem_passes<TMINOR, K1>(sg.all, m, 1, tpb, tw, sm);
       store_phase<TMINOR>(sm, d.n, tpb, s2);
     }
   }

@@ -1,5 +1,8 @@
 // Complex-input kernels: batched C2C rows and column tiles (the second
 // dimension of CFft2D), each with a mixed-radix or a fused Bluestein core.
+// Instantiated per dtype by k_complex_f32.cu / k_complex_f64.cu.
+#pragma once
+
 #include "kernels.cuh"
 
 namespace chfft {
@@ -42,8 +45,8 @@ struct RowStore {
   }
 };
 
-template <typename T, bool BLUE>
-__global__ void __launch_bounds__(kMaxThreads) k_c2c(const KArgs a) {
+template <typename T, bool BLUE, bool K1>
+__global__ void __launch_bounds__(kMaxThreads, K1 ? 2 : 1) k_c2c(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
@@ -51,7 +54,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_c2c(const KArgs a) {
   const int nvalid = (int)min((long long)a.tpb, a.count - t0);
   RowLoad<C> ld{(const C*)a.in + t0 * a.in_dist, a.in_dist, nvalid, (T)a.scale, a.back};
   RowStore<C> st{(C*)a.out + t0 * a.out_dist, a.out_dist, nvalid, a.back};
-  core_fft<BLUE, false, true>(a.core, a.tpb, sm, ld, st);
+  core_fft<BLUE, false, true, K1>(a.core, a.tpb, sm, ld, st);
 }
 
 // ---------------------------------------------------------------- columns
@@ -81,8 +84,8 @@ struct ColStore {
   }
 };
 
-template <typename T, bool BLUE>
-__global__ void __launch_bounds__(kMaxThreads) k_cols(const KArgs a) {
+template <typename T, bool BLUE, bool K1>
+__global__ void __launch_bounds__(kMaxThreads, K1 ? 2 : 1) k_cols(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
@@ -91,18 +94,23 @@ __global__ void __launch_bounds__(kMaxThreads) k_cols(const KArgs a) {
   const int nvalid = min(a.tpb, a.ncols - c0);
   ColLoad<C> ld{(const C*)a.in + tr * a.in_dist + c0, a.ncols, nvalid, (T)a.scale, a.back};
   ColStore<C> st{(C*)a.out + tr * a.out_dist + c0, a.ncols, nvalid, a.back};
-  core_fft<BLUE, true, !BLUE>(a.core, a.tpb, sm, ld, st);
+  core_fft<BLUE, true, true, K1>(a.core, a.tpb, sm, ld, st);
 }
 
 }  // namespace
 
 template <typename T>
-cudaError_t launch_complex(Kernel which, bool blue, const KArgs& a, unsigned blocks, unsigned threads, size_t smem,
-                           cudaStream_t stream) {
+cudaError_t launch_complex(Kernel which, bool blue, bool k1, const KArgs& a, unsigned blocks, unsigned threads,
+                           size_t smem, cudaStream_t stream) {
   void (*fn)(const KArgs) = nullptr;
   switch (which) {
-    case Kernel::C2C: fn = blue ? k_c2c<T, true> : k_c2c<T, false>; break;
-    case Kernel::COLS: fn = blue ? k_cols<T, true> : k_cols<T, false>; break;
+    case Kernel::C2C:
+      fn = blue ? (k1 ? k_c2c<T, true, true> : k_c2c<T, true, false>) : (k1 ? k_c2c<T, false, true> : k_c2c<T, false, false>);
+      break;
+    case Kernel::COLS:
+      fn = blue ? (k1 ? k_cols<T, true, true> : k_cols<T, true, false>)
+                : (k1 ? k_cols<T, false, true> : k_cols<T, false, false>);
+      break;
     default: return cudaErrorInvalidValue;
   }
   if (smem > 48 * 1024) {
@@ -112,8 +120,5 @@ cudaError_t launch_complex(Kernel which, bool blue, const KArgs& a, unsigned blo
   fn<<<blocks, threads, smem, stream>>>(a);
   return cudaGetLastError();
 }
-
-template cudaError_t launch_complex<float>(Kernel, bool, const KArgs&, unsigned, unsigned, size_t, cudaStream_t);
-template cudaError_t launch_complex<double>(Kernel, bool, const KArgs&, unsigned, unsigned, size_t, cudaStream_t);
 
 }  // namespace chfft

@@ -1,0 +1,6 @@
+// double instantiation of the complex-input kernels (k_complex.cuh).
+#include "k_complex.cuh"
+
+namespace chfft {
+template cudaError_t launch_complex<double>(Kernel, bool, bool, const KArgs&, unsigned, unsigned, size_t, cudaStream_t);
+}  // namespace chfft

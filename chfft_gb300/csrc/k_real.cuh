@@ -8,13 +8,12 @@
 // pass's loader and post-passes that need one FFT output per result live in
 // the last pass's storer. Split steps that pair bin k with bin h-k run as a
 // separate cooperative phase on the shared-memory tile.
+// Instantiated per dtype by k_real_f32.cu / k_real_f64.cu.
+#pragma once
+
 #include "kernels.cuh"
 
 namespace chfft {
-
-template <typename T>
-cudaError_t launch_complex(Kernel which, bool blue, const KArgs& a, unsigned blocks, unsigned threads, size_t smem,
-                           cudaStream_t stream);
 
 namespace {
 
@@ -48,15 +47,15 @@ struct PackLoad {
   }
 };
 
-template <typename T, bool BLUE>
-__global__ void __launch_bounds__(kMaxThreads) k_r2c(const KArgs a) {
+template <typename T, bool BLUE, bool K1>
+__global__ void __launch_bounds__(kMaxThreads, K1 ? 2 : 1) k_r2c(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
   const BlockRange br = block_range(a);
   const int h = a.core.n, N = 2 * h;
   PackLoad<T> ld{(const T*)a.in + br.t0 * a.in_dist, a.in_dist, br.nvalid, (T)a.scale};
-  core_fft<BLUE, false, false>(a.core, a.tpb, sm, ld, sm);
+  core_fft<BLUE, false, false, K1>(a.core, a.tpb, sm, ld, sm);
   // Split (src/rfft1d.rs:136-148): X_i = Z_i - x, X_{h-i} = Z_{h-i} + conj(x),
   // x = coef_i (Z_i - conj Z_{h-i}); DC / Nyquist / N/4 bins from item 0.
   const int qlen = (N + 3) >> 2;
@@ -94,8 +93,8 @@ struct UnpackStore {
   }
 };
 
-template <typename T, bool BLUE>
-__global__ void __launch_bounds__(kMaxThreads) k_c2r(const KArgs a) {
+template <typename T, bool BLUE, bool K1>
+__global__ void __launch_bounds__(kMaxThreads, K1 ? 2 : 1) k_c2r(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
@@ -120,7 +119,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_c2r(const KArgs a) {
   }
   __syncthreads();
   UnpackStore<T> st{(T*)a.out + br.t0 * a.out_dist, a.out_dist, br.nvalid, T(2.0 * a.scale)};
-  core_fft<BLUE, false, false>(a.core, a.tpb, sm, sm, st);
+  core_fft<BLUE, false, false, K1>(a.core, a.tpb, sm, sm, st);
 }
 
 // ---------------------------------------------------------------- DCT-II
@@ -146,15 +145,15 @@ struct DctPackLoad {
   }
 };
 
-template <typename T, bool BLUE>
-__global__ void __launch_bounds__(kMaxThreads) k_dct2(const KArgs a) {
+template <typename T, bool BLUE, bool K1>
+__global__ void __launch_bounds__(kMaxThreads, K1 ? 2 : 1) k_dct2(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
   const BlockRange br = block_range(a);
   const int h = a.core.n, N = 2 * h;
   DctPackLoad<T> ld{(const T*)a.in + br.t0 * a.in_dist, a.in_dist, br.nvalid, N, (T)a.scale, (T)a.aux_scalar};
-  core_fft<BLUE, false, false>(a.core, a.tpb, sm, ld, sm);
+  core_fft<BLUE, false, false, K1>(a.core, a.tpb, sm, ld, sm);
   // Post-twiddle with exp(+i pi k / 2N) (src/dct1d.rs:266-289).
   const int q2 = (N + 3) >> 2;
   const C* coef = (const C*)a.aux0;
@@ -214,8 +213,8 @@ struct DctUnpackStore {
   }
 };
 
-template <typename T, bool BLUE>
-__global__ void __launch_bounds__(kMaxThreads) k_dct3(const KArgs a) {
+template <typename T, bool BLUE, bool K1>
+__global__ void __launch_bounds__(kMaxThreads, K1 ? 2 : 1) k_dct3(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
@@ -244,7 +243,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_dct3(const KArgs a) {
   }
   __syncthreads();
   DctUnpackStore<T> st{(T*)a.out + br.t0 * a.out_dist, a.out_dist, br.nvalid, h};
-  core_fft<BLUE, false, false>(a.core, a.tpb, sm, sm, st);
+  core_fft<BLUE, false, false, K1>(a.core, a.tpb, sm, sm, st);
 }
 
 // ---------------------------------------------------------------- MDCT
@@ -303,8 +302,8 @@ struct MdctStore {
   }
 };
 
-template <typename T, bool BLUE>
-__global__ void __launch_bounds__(kMaxThreads) k_mdct(const KArgs a) {
+template <typename T, bool BLUE, bool K1>
+__global__ void __launch_bounds__(kMaxThreads, K1 ? 2 : 1) k_mdct(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
@@ -313,7 +312,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_mdct(const KArgs a) {
   const C* tw = (const C*)a.aux0;
   MdctLoad<T> ld{(const T*)a.in + br.t0 * a.in_dist, a.in_dist, br.nvalid, n, tw, (const T*)a.aux1};
   MdctStore<T> st{(T*)a.out + br.t0 * a.out_dist, a.out_dist, br.nvalid, n >> 1, tw, (T)a.scale};
-  core_fft<BLUE, false, false>(a.core, a.tpb, sm, ld, st);
+  core_fft<BLUE, false, false, K1>(a.core, a.tpb, sm, ld, st);
 }
 
 // IMDCT: pre-twiddle x(-2) (src/mdct1d.rs:259-263), FORWARD N/4 FFT, then
@@ -361,8 +360,8 @@ struct ImdctStore {
   }
 };
 
-template <typename T, bool BLUE>
-__global__ void __launch_bounds__(kMaxThreads) k_imdct(const KArgs a) {
+template <typename T, bool BLUE, bool K1>
+__global__ void __launch_bounds__(kMaxThreads, K1 ? 2 : 1) k_imdct(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
@@ -371,26 +370,26 @@ __global__ void __launch_bounds__(kMaxThreads) k_imdct(const KArgs a) {
   const C* tw = (const C*)a.aux0;
   ImdctLoad<T> ld{(const T*)a.in + br.t0 * a.in_dist, a.in_dist, br.nvalid, n >> 1, tw};
   ImdctStore<T> st{(T*)a.out + br.t0 * a.out_dist, a.out_dist, br.nvalid, n, tw, (const T*)a.aux1, (T)a.scale};
-  core_fft<BLUE, false, false>(a.core, a.tpb, sm, ld, st);
+  core_fft<BLUE, false, false, K1>(a.core, a.tpb, sm, ld, st);
 }
 
 }  // namespace
 
 template <typename T>
-cudaError_t launch_kernel(Kernel which, bool blue, const KArgs& a, unsigned blocks, unsigned threads, size_t smem,
-                          cudaStream_t stream) {
+cudaError_t launch_real(Kernel which, bool blue, bool k1, const KArgs& a, unsigned blocks, unsigned threads,
+                        size_t smem, cudaStream_t stream) {
   void (*fn)(const KArgs) = nullptr;
+#define CHFFT_PICK(K) (blue ? (k1 ? K<T, true, true> : K<T, true, false>) : (k1 ? K<T, false, true> : K<T, false, false>))
   switch (which) {
-    case Kernel::C2C:
-    case Kernel::COLS: return launch_complex<T>(which, blue, a, blocks, threads, smem, stream);
-    case Kernel::R2C: fn = blue ? k_r2c<T, true> : k_r2c<T, false>; break;
-    case Kernel::C2R: fn = blue ? k_c2r<T, true> : k_c2r<T, false>; break;
-    case Kernel::DCT2: fn = blue ? k_dct2<T, true> : k_dct2<T, false>; break;
-    case Kernel::DCT3: fn = blue ? k_dct3<T, true> : k_dct3<T, false>; break;
-    case Kernel::MDCT: fn = blue ? k_mdct<T, true> : k_mdct<T, false>; break;
-    case Kernel::IMDCT: fn = blue ? k_imdct<T, true> : k_imdct<T, false>; break;
+    case Kernel::R2C: fn = CHFFT_PICK(k_r2c); break;
+    case Kernel::C2R: fn = CHFFT_PICK(k_c2r); break;
+    case Kernel::DCT2: fn = CHFFT_PICK(k_dct2); break;
+    case Kernel::DCT3: fn = CHFFT_PICK(k_dct3); break;
+    case Kernel::MDCT: fn = CHFFT_PICK(k_mdct); break;
+    case Kernel::IMDCT: fn = CHFFT_PICK(k_imdct); break;
+    default: return cudaErrorInvalidValue;
   }
-  if (!fn) return cudaErrorInvalidValue;
+#undef CHFFT_PICK
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -398,8 +397,5 @@ cudaError_t launch_kernel(Kernel which, bool blue, const KArgs& a, unsigned bloc
   fn<<<blocks, threads, smem, stream>>>(a);
   return cudaGetLastError();
 }
-
-template cudaError_t launch_kernel<float>(Kernel, bool, const KArgs&, unsigned, unsigned, size_t, cudaStream_t);
-template cudaError_t launch_kernel<double>(Kernel, bool, const KArgs&, unsigned, unsigned, size_t, cudaStream_t);
 
 }  // namespace chfft

@@ -43,10 +43,17 @@ enum class Kernel : int {
 
 // Launch `which` for dtype T (float or double) with `blocks` CTAs of
 // `threads` threads and `smem` bytes of dynamic shared memory; `blue`
-// selects the Bluestein core.
+// selects the Bluestein core and `k1` the one-butterfly-per-thread variant.
 template <typename T>
-cudaError_t launch_kernel(Kernel which, bool blue, const KArgs& a, unsigned blocks, unsigned threads, size_t smem,
-                          cudaStream_t stream);
+cudaError_t launch_kernel(Kernel which, bool blue, bool k1, const KArgs& a, unsigned blocks, unsigned threads,
+                          size_t smem, cudaStream_t stream);
+// Per-family launchers (k_complex_*.cu, k_real_*.cu), dispatched by launch_kernel.
+template <typename T>
+cudaError_t launch_complex(Kernel which, bool blue, bool k1, const KArgs& a, unsigned blocks, unsigned threads,
+                           size_t smem, cudaStream_t stream);
+template <typename T>
+cudaError_t launch_real(Kernel which, bool blue, bool k1, const KArgs& a, unsigned blocks, unsigned threads,
+                        size_t smem, cudaStream_t stream);
 
 // Table generators (FP64 arithmetic, stored in the working dtype T).
 enum class Table : int {

@@ -102,12 +102,12 @@ bool make_stages(long long n, StageList* out) {
   return true;
 }
 
-int threads_needed(const StageList& st, int ept, int tpb) {
+int threads_needed(const StageList& st, int ept, int tpb, bool k1) {
   long long need = 1;
   for (int i = 0; i < kNumRadix; i++) {
     if (st.all[i] == 0) continue;
     int r = radix_at(i);
-    long long k = ept / r;
+    long long k = k1 ? 1 : ept / r;
     long long nb = (long long)tpb * (st.n / r);
     need = std::max(need, (nb + k - 1) / k);
   }
@@ -198,7 +198,7 @@ bool Core::build(long long n_, int dtype_, cudaStream_t s) {
     a.out = bhat.p;
     a.scale = 1.0;
     a.in_dist = a.out_dist = m;
-    CHFFT_CUDA(launch_kernel<float>(Kernel::C2C, false, a, 1, g.threads, g.smem, s));
+    CHFFT_CUDA(launch_kernel<float>(Kernel::C2C, false, g.k1, a, 1, g.threads, g.smem, s));
   }
   CHFFT_CUDA(cudaStreamSynchronize(s));  // temporaries are freed on return
   return true;
@@ -225,7 +225,7 @@ static void fft_f64_inplace(double2* d_data, const Core& c64, cudaStream_t s) {
   a.out = d_data;
   a.scale = 1.0;
   a.in_dist = a.out_dist = c64.st.n;
-  CHFFT_CUDA(launch_kernel<double>(Kernel::C2C, false, a, 1, g.threads, g.smem, s));
+  CHFFT_CUDA(launch_kernel<double>(Kernel::C2C, false, g.k1, a, 1, g.threads, g.smem, s));
 }
 
 Geo row_geo(const Core& c, long long count, int target_threads) {
@@ -234,16 +234,27 @@ Geo row_geo(const Core& c, long long count, int target_threads) {
   const int m = c.st.n;
   g.ld = smem_ld(m);
   const size_t per = (size_t)g.ld * cplx_bytes(c.dtype);
-  const int t1 = std::max(1, threads_needed(c.st, ept, 1));
-  int tpb = std::max(1, target_threads / t1);
-  tpb = (int)std::min<size_t>(tpb, std::max<size_t>(1, (64 * 1024) / per));
-  tpb = (int)std::max<long long>(1, std::min<long long>(tpb, count));
-  while (tpb > 1 && threads_needed(c.st, ept, tpb) > kMaxThreads) tpb--;
-  g.tpb = tpb;
-  int th = threads_needed(c.st, ept, tpb);
+  const int t1k = std::max(1, threads_needed(c.st, ept, 1, true));
+  if (t1k <= kMaxThreads) {
+    // One butterfly per thread: fill the CTA up to 512 threads, keeping two
+    // CTAs' tiles within an SM's shared memory.
+    g.k1 = true;
+    int tpb = std::max(1, kMaxThreads / t1k);
+    tpb = (int)std::min<size_t>(tpb, std::max<size_t>(1, (kMaxSmem / 2) / per));
+    tpb = (int)std::max<long long>(1, std::min<long long>(tpb, count));
+    g.tpb = tpb;
+  } else {
+    const int t1 = std::max(1, threads_needed(c.st, ept, 1));
+    int tpb = std::max(1, target_threads / t1);
+    tpb = (int)std::min<size_t>(tpb, std::max<size_t>(1, (64 * 1024) / per));
+    tpb = (int)std::max<long long>(1, std::min<long long>(tpb, count));
+    while (tpb > 1 && threads_needed(c.st, ept, tpb) > kMaxThreads) tpb--;
+    g.tpb = tpb;
+  }
+  int th = threads_needed(c.st, ept, g.tpb, g.k1);
   th = std::max(32, ((th + 31) / 32) * 32);
   g.threads = std::min(th, kMaxThreads);
-  g.smem = (size_t)tpb * per;
+  g.smem = (size_t)g.tpb * per;
   return g;
 }
 
@@ -256,7 +267,8 @@ Geo col_geo(const Core& c, int ncols) {
   tpb = std::min(tpb, std::max(1, ncols));
   while (tpb > 1 && ((size_t)tpb * per > kMaxSmem || threads_needed(c.st, ept, tpb) > kMaxThreads)) tpb--;
   g.tpb = tpb;
-  int th = threads_needed(c.st, ept, tpb);
+  g.k1 = threads_needed(c.st, ept, tpb, true) <= kMaxThreads;
+  int th = threads_needed(c.st, ept, tpb, g.k1);
   th = std::max(32, ((th + 31) / 32) * 32);
   g.threads = std::min(th, kMaxThreads);
   g.smem = (size_t)tpb * per;

@@ -62,8 +62,9 @@ Smooth factor_smooth(long long n);
 // Stage list for a 7-smooth n (fewest passes; radices 16/8/4/2/10/5/3/7).
 // Returns false when n is not 7-smooth.
 bool make_stages(long long n, StageList* out);
-// Threads a CTA needs to run `tpb` sequences with these stages.
-int threads_needed(const StageList& st, int ept, int tpb);
+// Threads a CTA needs to run `tpb` sequences with these stages (k1: one
+// butterfly per thread per pass; otherwise up to EPT/R per thread).
+int threads_needed(const StageList& st, int ept, int tpb, bool k1 = false);
 // Whether one sequence of these stages fits a CTA (threads and shared memory).
 bool fits_cta(const StageList& st, int dtype);
 
@@ -86,6 +87,7 @@ struct Geo {
   int tpb = 1, threads = 32;
   size_t smem = 0;
   int ld = 0;
+  bool k1 = false;  // one-butterfly-per-thread kernel variant
 };
 Geo row_geo(const Core& c, long long count, int target_threads = 256);
 Geo col_geo(const Core& c, int ncols);
