@@ -103,6 +103,8 @@ def lib() -> ctypes.CDLL:
     for name in ("chfft_last_error", "chfft_status_string", "chfft_version"):
         getattr(L, name).restype = ctypes.c_char_p
     L.chfft_status_string.argtypes = [ctypes.c_int]
+    L.chfft_plan_compiler_available.restype = ctypes.c_int
+    L.chfft_plan_compiler_cache_size.restype = ctypes.c_size_t
     _lib = L
     return L
 
@@ -118,6 +120,16 @@ def _check(rc: int):
 
 def version() -> str:
     return lib().chfft_version().decode()
+
+
+def plan_compiler_available() -> bool:
+    """Whether plan-time specialised kernels (NVRTC) can be used (CHFFT_JIT selects when)."""
+    return bool(lib().chfft_plan_compiler_available())
+
+
+def plan_compiler_cache_size() -> int:
+    """Specialised kernels compiled so far in this process."""
+    return int(lib().chfft_plan_compiler_cache_size())
 
 
 def _dtype_id(dtype) -> int:

@@ -19,7 +19,27 @@ LIB = os.path.join(LIBDIR, "libchfft_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden", "-I", INCLUDE]
+FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden", "-I", INCLUDE, "-I", BUILD]
+# Kernel headers the plan-time compiler (csrc/jit.cu) hands to NVRTC.
+JIT_HEADERS = ["common.cuh", "engine.cuh", "kernels.cuh", "k_complex.cuh", "k_real.cuh"]
+
+
+def _gen_jit_headers() -> None:
+    """Write _build/jit_headers.inc: the kernel headers as C++ raw strings."""
+    names, srcs = [], []
+    for h in JIT_HEADERS:
+        text = open(os.path.join(CSRC, h)).read()
+        if ")CHFFT_SRC\"" in text:
+            raise RuntimeError(f"{h} contains the raw-string delimiter")
+        names.append(f'"{h}"')
+        srcs.append('R"CHFFT_SRC(' + text + ')CHFFT_SRC"')
+    body = (f"static const int kJitHeaderCount = {len(JIT_HEADERS)};\n"
+            f"static const char* const kJitHeaderNames[] = {{{', '.join(names)}}};\n"
+            f"static const char* const kJitHeaderSrc[] = {{\n" + ",\n".join(srcs) + "};\n")
+    out = os.path.join(BUILD, "jit_headers.inc")
+    if not os.path.exists(out) or open(out).read() != body:
+        with open(out, "w") as f:
+            f.write(body)
 
 
 def _nvcc() -> str:
@@ -62,6 +82,7 @@ def build(force: bool = False, jobs: int | None = None) -> str:
         for f in os.listdir(BUILD):
             if f.endswith(".o"):
                 os.remove(os.path.join(BUILD, f))
+    _gen_jit_headers()
     hm = max(os.path.getmtime(h) for h in _headers())
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=jobs or min(len(srcs), os.cpu_count() or 4)) as ex:

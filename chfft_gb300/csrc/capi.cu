@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "../../include/chfft_gpu.h"
+#include "jit.hpp"
 #include "plan.hpp"
 
 namespace chfft {
@@ -204,6 +205,22 @@ struct PlanImpl {
     return 1.0;
   }
 
+  // Plan-time specialised kernel when the plan compiler is on for this batch
+  // size (CHFFT_JIT: auto = batches of >= 2^18 elements), else the library
+  // kernel with run-time stages.
+  template <typename T>
+  void dispatch(Kernel k, const Core& c, const Geo& g, const KArgs& a, unsigned blocks, long long elems,
+                cudaStream_t s) {
+    const JitMode mode = jit_mode();
+    const bool want = c.st.n > 1 && (mode == JitMode::ALWAYS || (mode == JitMode::AUTO && elems >= (1LL << 18)));
+    if (want) {
+      int r = jit_launch(k, dtype, c, g, a, blocks, s);
+      if (r == 0) return;
+      if (r == 2) throw Fail{CHFFT_ECUDA, "launch of a plan-time specialised kernel failed"};
+    }
+    CHFFT_CUDA(launch_kernel<T>(k, c.blue, g.k1, a, blocks, g.threads, g.smem, s));
+  }
+
   template <typename T>
   void launch(Kernel k, const Core& c, KArgs& a, long long count, cudaStream_t s) {
     Geo g = row_geo(c, count);
@@ -212,7 +229,7 @@ struct PlanImpl {
     a.ld = g.ld;
     a.count = count;
     unsigned blocks = (unsigned)((count + g.tpb - 1) / g.tpb);
-    CHFFT_CUDA(launch_kernel<T>(k, c.blue, g.k1, a, blocks, g.threads, g.smem, s));
+    dispatch<T>(k, c, g, a, blocks, count * c.n, s);
   }
 
   template <typename T>
@@ -253,8 +270,7 @@ struct PlanImpl {
         b.scale = sc;
         b.in_dist = b.out_dist = len_m * len_n;
         b.ncols = (int)len_n;
-        CHFFT_CUDA(launch_kernel<T>(Kernel::COLS, core2.blue, g.k1, b, (unsigned)(batch * b.tiles_per_tr), g.threads,
-                                    g.smem, s));
+        dispatch<T>(Kernel::COLS, core2, g, b, (unsigned)(batch * b.tiles_per_tr), batch * len_m * len_n, s);
         return;
       }
       case CHFFT_KIND_RFFT1D:
@@ -705,5 +721,14 @@ const char* chfft_status_string(int status) {
 }
 
 const char* chfft_version(void) { return "chfft_gb300 0.1.0 (sm_103a)"; }
+
+int chfft_plan_compiler_available(void) {
+  std::string why;
+  if (chfft::jit_available(&why)) return 1;
+  chfft::tl_error = why;
+  return 0;
+}
+
+size_t chfft_plan_compiler_cache_size(void) { return chfft::jit_cache_size(); }
 
 }  // extern "C"

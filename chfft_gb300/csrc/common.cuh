@@ -6,12 +6,19 @@
 // (src/cfft1d.rs:270 takes &[Complex<T>]).
 #pragma once
 
+// The kernel headers also compile under NVRTC (plan-time specialised
+// kernels), which provides the CUDA vector types itself.
+#ifndef __CUDACC_RTC__
 #include <cuda_runtime.h>
 #include <stdint.h>
+#endif
 
 #define CHFFT_HD __host__ __device__ __forceinline__
 
 namespace chfft {
+
+template <class A, class B> struct same_type { static constexpr bool value = false; };
+template <class A> struct same_type<A, A> { static constexpr bool value = true; };
 
 template <typename T> struct Cx;
 template <> struct Cx<float> { using type = float2; };
@@ -32,6 +39,10 @@ template <typename C> CHFFT_HD C cmul(C a, C b) { return mk(a.x * b.x - a.y * b.
 template <typename C> CHFFT_HD C cmulc(C a, C b) { return mk(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y); }
 template <typename C, typename R> CHFFT_HD C cscale(C a, R s) { return mk(a.x * s, a.y * s); }
 template <typename C> CHFFT_HD C cconj(C a) { return mk(a.x, -a.y); }
+template <typename C> CHFFT_HD C czero() {
+  using R = typename Real<C>::type;
+  return mk(R(0), R(0));
+}
 // a * (-i) and a * i
 template <typename C> CHFFT_HD C mul_mi(C a) { return mk(a.y, -a.x); }
 template <typename C> CHFFT_HD C mul_pi(C a) { return mk(-a.y, a.x); }
@@ -201,7 +212,7 @@ template <> struct Dft<7> {
 
 // Composite R = A*B (A the divisor nearest sqrt(R)): with n = q + A*p and
 // k = k1 + B*k2, y_k = sum_q w_A^{q k2} w_R^{q k1} sum_p x_{q+Ap} w_B^{p k1}.
-template <int R> constexpr int split_a() {
+template <int R> __host__ __device__ constexpr int split_a() {
   int best = 1;
   for (int a = 2; a * a <= R; a++)
     if (R % a == 0) best = a;

@@ -22,8 +22,6 @@
 // consecutive threads walk adjacent sequences, which coalesces column tiles.
 #pragma once
 
-#include <type_traits>
-
 #include "common.cuh"
 
 namespace chfft {
@@ -243,8 +241,8 @@ __device__ __forceinline__ void core_fft(const CoreDesc& d, int tpb, const SmemI
   const StageList& sg = d.st;
   const int m = sg.n;
   if constexpr (!BLUE) {
-    constexpr bool kLoad = !std::is_same<Ld, SmemIO<C>>::value;
-    constexpr bool kStore = !std::is_same<St, SmemIO<C>>::value;
+    constexpr bool kLoad = !same_type<Ld, SmemIO<C>>::value;
+    constexpr bool kStore = !same_type<St, SmemIO<C>>::value;
     if (FUSED && kLoad && kStore && sg.npass >= 2) {
       pass_any<TMINOR, K1>(sg.rf, m, 1, tpb, tw, ld, sm);
       const int Ns = smem_passes<TMINOR, K1>(sg.mid, m, sg.rf, tpb, tw, sm);
@@ -280,5 +278,67 @@ __device__ __forceinline__ void core_fft(const CoreDesc& d, int tpb, const SmemI
     }
   }
 }
+
+// ---------------------------------------------------------------------------
+// Core policies. Every transform kernel is a template over one of these:
+//   DynCore  - stage list read at run time (the kernels compiled into the
+//              library, one per kind / dtype / variant);
+//   StatCore - stage list, lengths, sequences per CTA and tile stride fixed
+//              at compile time (kernels the plan compiler emits for one plan
+//              and compiles at plan time), so every index computation folds
+//              to constants and each pass is straight-line code.
+template <bool BLUE, bool TMINOR, bool FUSED, bool K1>
+struct DynCore {
+  static constexpr bool kK1 = K1;
+  template <typename C, class Ld, class St>
+  __device__ __forceinline__ static void run(const CoreDesc& d, int tpb, const SmemIO<C>& sm, const Ld& ld,
+                                             const St& st) {
+    core_fft<BLUE, TMINOR, FUSED, K1>(d, tpb, sm, ld, st);
+  }
+};
+
+// Passes R, Rest... with Ns = NS at the first: `ld` feeds the first pass,
+// `st` takes the last, the tile carries everything in between.
+template <int N, int TPB, int LD, bool TMINOR, bool K1, int NS, int R, int... Rest, typename C, class Ld, class St>
+__device__ __forceinline__ void static_passes(const C* tw, C* s, const Ld& ld, const St& st) {
+  if constexpr (sizeof...(Rest) == 0) {
+    pass_body<R, TMINOR, K1>(N, NS, TPB, tw, ld, st);
+  } else {
+    const SmemIO<C> sm{s, LD};
+    pass_body<R, TMINOR, K1>(N, NS, TPB, tw, ld, sm);
+    static_passes<N, TPB, LD, TMINOR, K1, NS * R, Rest...>(tw, s, sm, st);
+  }
+}
+
+template <bool BLUE, bool TMINOR, bool K1, int M, int NU, int TPB, int LD, int... Rs>
+struct StatCore {
+  static constexpr bool kK1 = K1;
+  template <typename C, class Ld, class St>
+  __device__ __forceinline__ static void run(const CoreDesc& d, int, const SmemIO<C>& sm0, const Ld& ld,
+                                             const St& st) {
+    const C* tw = static_cast<const C*>(d.tw);
+    const SmemIO<C> sm{sm0.s, LD};
+    constexpr bool kLoad = !same_type<Ld, SmemIO<C>>::value;
+    constexpr bool kStore = !same_type<St, SmemIO<C>>::value;
+    if constexpr (!BLUE) {
+      if constexpr (kLoad && kStore) {
+        static_passes<M, TPB, LD, TMINOR, K1, 1, Rs...>(tw, sm.s, ld, st);
+      } else if constexpr (kLoad) {
+        static_passes<M, TPB, LD, TMINOR, K1, 1, Rs...>(tw, sm.s, ld, sm);
+      } else if constexpr (kStore) {
+        static_passes<M, TPB, LD, TMINOR, K1, 1, Rs...>(tw, sm.s, sm, st);
+      } else {
+        static_passes<M, TPB, LD, TMINOR, K1, 1, Rs...>(tw, sm.s, sm, sm);
+      }
+    } else {
+      const C* chirp = static_cast<const C*>(d.chirp);
+      ChirpIn<C, Ld> l1{ld, chirp, NU};
+      ChirpOut<C, St> s2{st, chirp, NU};
+      static_passes<M, TPB, LD, TMINOR, K1, 1, Rs...>(tw, sm.s, l1, sm);
+      spectrum_phase<TMINOR>(sm, M, TPB, static_cast<const C*>(d.bhat));
+      static_passes<M, TPB, LD, TMINOR, K1, 1, Rs...>(tw, sm.s, sm, s2);
+    }
+  }
+};
 
 }  // namespace chfft

@@ -1,0 +1,240 @@
+// Plan-time kernel specialisation.
+//
+// The plan compiler emits, for one plan, the kernel template of its kind
+// instantiated with a StatCore: FFT length, Bluestein length, sequences per
+// CTA, tile stride and the exact radix sequence become template constants,
+// so the pass bodies compile to straight-line code with constant indices
+// and strides. The instance is compiled with NVRTC for sm_103a at first use
+// and cached per process (and per device). NVRTC and the CUDA driver API are
+// opened with dlopen on first use, so the library itself loads on hosts
+// without a GPU or without NVRTC; when either is missing the plan keeps the
+// run-time-stage kernels compiled into the library.
+#include <dlfcn.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "jit.hpp"
+#include "jit_headers.inc"  // generated by _build.py: kernel headers as strings
+
+namespace chfft {
+namespace {
+
+typedef int CUresult;
+typedef struct CUmod_st* CUmodule;
+typedef struct CUfunc_st* CUfunction;
+typedef struct CUstream_st* CUstream;
+typedef int nvrtcResult;
+typedef struct _nvrtcProgram* nvrtcProgram;
+constexpr int kAttrMaxDynSmem = 8;  // CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES
+
+struct Api {
+  bool tried = false, ok = false;
+  std::string why;
+  CUresult (*cuModuleLoadData)(CUmodule*, const void*) = nullptr;
+  CUresult (*cuModuleGetFunction)(CUfunction*, CUmodule, const char*) = nullptr;
+  CUresult (*cuLaunchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned,
+                             CUstream, void**, void**) = nullptr;
+  CUresult (*cuFuncSetAttribute)(CUfunction, int, int) = nullptr;
+  nvrtcResult (*nvrtcCreateProgram)(nvrtcProgram*, const char*, const char*, int, const char* const*,
+                                    const char* const*) = nullptr;
+  nvrtcResult (*nvrtcAddNameExpression)(nvrtcProgram, const char*) = nullptr;
+  nvrtcResult (*nvrtcCompileProgram)(nvrtcProgram, int, const char* const*) = nullptr;
+  nvrtcResult (*nvrtcGetLoweredName)(nvrtcProgram, const char*, const char**) = nullptr;
+  nvrtcResult (*nvrtcGetCUBINSize)(nvrtcProgram, size_t*) = nullptr;
+  nvrtcResult (*nvrtcGetCUBIN)(nvrtcProgram, char*) = nullptr;
+  nvrtcResult (*nvrtcGetProgramLogSize)(nvrtcProgram, size_t*) = nullptr;
+  nvrtcResult (*nvrtcGetProgramLog)(nvrtcProgram, char*) = nullptr;
+  nvrtcResult (*nvrtcDestroyProgram)(nvrtcProgram*) = nullptr;
+};
+
+Api g_api;
+std::mutex g_mu;
+
+struct Entry {
+  CUfunction fn = nullptr;
+  int smem_set = 0;
+  bool failed = false;
+};
+std::unordered_map<std::string, Entry> g_cache;
+
+template <class F>
+bool sym(void* h, const char* name, F* out) {
+  *out = reinterpret_cast<F>(dlsym(h, name));
+  return *out != nullptr;
+}
+
+bool load_api() {
+  if (g_api.tried) return g_api.ok;
+  g_api.tried = true;
+  void* cu = dlopen("libcuda.so.1", RTLD_NOW | RTLD_GLOBAL);
+  if (!cu) {
+    g_api.why = "libcuda.so.1 not found";
+    return false;
+  }
+  void* rtc = nullptr;
+  const char* cands[] = {"libnvrtc.so.13", "libnvrtc.so", "/usr/local/cuda/lib64/libnvrtc.so.13",
+                         "/usr/local/cuda/lib64/libnvrtc.so"};
+  for (const char* c : cands)
+    if ((rtc = dlopen(c, RTLD_NOW | RTLD_GLOBAL))) break;
+  if (!rtc) {
+    g_api.why = "libnvrtc not found";
+    return false;
+  }
+  bool ok = sym(cu, "cuModuleLoadData", &g_api.cuModuleLoadData) &&
+            sym(cu, "cuModuleGetFunction", &g_api.cuModuleGetFunction) &&
+            sym(cu, "cuLaunchKernel", &g_api.cuLaunchKernel) &&
+            sym(cu, "cuFuncSetAttribute", &g_api.cuFuncSetAttribute) &&
+            sym(rtc, "nvrtcCreateProgram", &g_api.nvrtcCreateProgram) &&
+            sym(rtc, "nvrtcAddNameExpression", &g_api.nvrtcAddNameExpression) &&
+            sym(rtc, "nvrtcCompileProgram", &g_api.nvrtcCompileProgram) &&
+            sym(rtc, "nvrtcGetLoweredName", &g_api.nvrtcGetLoweredName) &&
+            sym(rtc, "nvrtcGetCUBINSize", &g_api.nvrtcGetCUBINSize) &&
+            sym(rtc, "nvrtcGetCUBIN", &g_api.nvrtcGetCUBIN) &&
+            sym(rtc, "nvrtcGetProgramLogSize", &g_api.nvrtcGetProgramLogSize) &&
+            sym(rtc, "nvrtcGetProgramLog", &g_api.nvrtcGetProgramLog) &&
+            sym(rtc, "nvrtcDestroyProgram", &g_api.nvrtcDestroyProgram);
+  if (!ok) {
+    g_api.why = "missing NVRTC / driver entry points";
+    return false;
+  }
+  g_api.ok = true;
+  return true;
+}
+
+const char* kernel_template(Kernel k) {
+  switch (k) {
+    case Kernel::C2C: return "chfft::kern::k_c2c";
+    case Kernel::COLS: return "chfft::kern::k_cols";
+    case Kernel::R2C: return "chfft::kern::k_r2c";
+    case Kernel::C2R: return "chfft::kern::k_c2r";
+    case Kernel::DCT2: return "chfft::kern::k_dct2";
+    case Kernel::DCT3: return "chfft::kern::k_dct3";
+    case Kernel::MDCT: return "chfft::kern::k_mdct";
+    case Kernel::IMDCT: return "chfft::kern::k_imdct";
+  }
+  return "";
+}
+
+// Radices in the order the fused path runs them (rf, mid..., rl), or the
+// canonical order when the list has fewer than two passes.
+std::vector<int> pass_order(const StageList& st) {
+  std::vector<int> r;
+  if (st.npass >= 2) {
+    r.push_back(st.rf);
+    for (int i = 0; i < kNumRadix; i++)
+      for (int c = 0; c < st.mid[i]; c++) r.push_back(radix_at(i));
+    r.push_back(st.rl);
+  } else {
+    for (int i = 0; i < kNumRadix; i++)
+      for (int c = 0; c < st.all[i]; c++) r.push_back(radix_at(i));
+  }
+  return r;
+}
+
+std::string name_expression(Kernel k, int dtype, const Core& c, const Geo& g) {
+  std::string s = "&";
+  s += kernel_template(k);
+  s += dtype == 0 ? "<float, " : "<double, ";
+  s += "chfft::StatCore<";
+  s += c.blue ? "true," : "false,";
+  s += k == Kernel::COLS ? "true," : "false,";
+  s += g.k1 ? "true," : "false,";
+  s += std::to_string(c.st.n) + "," + std::to_string(c.n) + "," + std::to_string(g.tpb) + "," + std::to_string(g.ld);
+  for (int r : pass_order(c.st)) s += "," + std::to_string(r);
+  s += ">>";
+  return s;
+}
+
+bool compile(const std::string& expr, Entry* e, std::string* log) {
+  nvrtcProgram prog = nullptr;
+  const char* src = "#include \"k_complex.cuh\"\n#include \"k_real.cuh\"\n";
+  if (g_api.nvrtcCreateProgram(&prog, src, "chfft_plan.cu", kJitHeaderCount, kJitHeaderSrc, kJitHeaderNames) != 0) {
+    *log = "nvrtcCreateProgram failed";
+    return false;
+  }
+  g_api.nvrtcAddNameExpression(prog, expr.c_str());
+  const char* opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "-lineinfo", "-DCHFFT_PLAN_TIME=1"};
+  nvrtcResult rc = g_api.nvrtcCompileProgram(prog, 4, opts);
+  if (rc != 0) {
+    size_t n = 0;
+    g_api.nvrtcGetProgramLogSize(prog, &n);
+    log->assign(n, '\0');
+    if (n) g_api.nvrtcGetProgramLog(prog, &(*log)[0]);
+    g_api.nvrtcDestroyProgram(&prog);
+    return false;
+  }
+  const char* lowered = nullptr;
+  g_api.nvrtcGetLoweredName(prog, expr.c_str(), &lowered);
+  std::string lname = lowered ? lowered : "";
+  size_t sz = 0;
+  g_api.nvrtcGetCUBINSize(prog, &sz);
+  std::vector<char> cubin(sz);
+  g_api.nvrtcGetCUBIN(prog, cubin.data());
+  g_api.nvrtcDestroyProgram(&prog);
+  CUmodule mod = nullptr;
+  if (g_api.cuModuleLoadData(&mod, cubin.data()) != 0 || g_api.cuModuleGetFunction(&e->fn, mod, lname.c_str()) != 0) {
+    *log = "module load failed";
+    e->fn = nullptr;
+    return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+JitMode jit_mode() {
+  const char* v = std::getenv("CHFFT_JIT");
+  if (!v || !*v || !std::strcmp(v, "auto")) return JitMode::AUTO;
+  if (!std::strcmp(v, "0") || !std::strcmp(v, "off")) return JitMode::OFF;
+  return JitMode::ALWAYS;
+}
+
+bool jit_available(std::string* why) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  bool ok = load_api();
+  if (!ok && why) *why = g_api.why;
+  return ok;
+}
+
+int jit_launch(Kernel k, int dtype, const Core& c, const Geo& g, const KArgs& a, unsigned blocks,
+               cudaStream_t stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!load_api()) return 1;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const std::string expr = name_expression(k, dtype, c, g);
+  Entry& e = g_cache[std::to_string(dev) + "|" + expr];
+  if (e.failed) return 1;
+  if (!e.fn) {
+    std::string log;
+    if (!compile(expr, &e, &log)) {
+      e.failed = true;
+      if (std::getenv("CHFFT_JIT_VERBOSE")) fprintf(stderr, "chfft plan-time compile failed for %s:\n%s\n", expr.c_str(), log.c_str());
+      return 1;
+    }
+  }
+  if ((int)g.smem > 48 * 1024 && e.smem_set < (int)g.smem) {
+    if (g_api.cuFuncSetAttribute(e.fn, kAttrMaxDynSmem, (int)g.smem) != 0) return 2;
+    e.smem_set = (int)g.smem;
+  }
+  void* args[] = {const_cast<KArgs*>(&a)};
+  if (g_api.cuLaunchKernel(e.fn, blocks, 1, 1, g.threads, 1, 1, (unsigned)g.smem, (CUstream)stream, args, nullptr) != 0)
+    return 2;
+  return 0;
+}
+
+size_t jit_cache_size() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  size_t n = 0;
+  for (auto& kv : g_cache)
+    if (kv.second.fn) n++;
+  return n;
+}
+
+}  // namespace chfft

@@ -1,19 +1,15 @@
 // Complex-input kernels: batched C2C rows and column tiles (the second
 // dimension of CFft2D), each with a mixed-radix or a fused Bluestein core.
-// Instantiated per dtype by k_complex_f32.cu / k_complex_f64.cu.
+// Each kernel is a template over a core policy (engine.cuh): k_complex_f32.cu
+// / k_complex_f64.cu instantiate the run-time-stage kernels, the plan-time
+// compiler (jit.cu) instantiates compile-time-stage ones.
 #pragma once
 
 #include "kernels.cuh"
 
 namespace chfft {
 
-namespace {
-
-template <typename C>
-__device__ __forceinline__ C czero() {
-  using R = typename Real<C>::type;
-  return mk(R(0), R(0));
-}
+namespace kern {
 
 // ---------------------------------------------------------------- rows
 // Contiguous sequences. The backward transform conjugates on the way in and
@@ -45,8 +41,8 @@ struct RowStore {
   }
 };
 
-template <typename T, bool BLUE, bool K1>
-__global__ void __launch_bounds__(kMaxThreads, K1 ? 2 : 1) k_c2c(const KArgs a) {
+template <typename T, class CoreT>
+__global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_c2c(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
@@ -54,7 +50,7 @@ __global__ void __launch_bounds__(kMaxThreads, K1 ? 2 : 1) k_c2c(const KArgs a) 
   const int nvalid = (int)min((long long)a.tpb, a.count - t0);
   RowLoad<C> ld{(const C*)a.in + t0 * a.in_dist, a.in_dist, nvalid, (T)a.scale, a.back};
   RowStore<C> st{(C*)a.out + t0 * a.out_dist, a.out_dist, nvalid, a.back};
-  core_fft<BLUE, false, true, K1>(a.core, a.tpb, sm, ld, st);
+  CoreT::run(a.core, a.tpb, sm, ld, st);
 }
 
 // ---------------------------------------------------------------- columns
@@ -84,8 +80,8 @@ struct ColStore {
   }
 };
 
-template <typename T, bool BLUE, bool K1>
-__global__ void __launch_bounds__(kMaxThreads, K1 ? 2 : 1) k_cols(const KArgs a) {
+template <typename T, class CoreT>
+__global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_cols(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
@@ -94,25 +90,26 @@ __global__ void __launch_bounds__(kMaxThreads, K1 ? 2 : 1) k_cols(const KArgs a)
   const int nvalid = min(a.tpb, a.ncols - c0);
   ColLoad<C> ld{(const C*)a.in + tr * a.in_dist + c0, a.ncols, nvalid, (T)a.scale, a.back};
   ColStore<C> st{(C*)a.out + tr * a.out_dist + c0, a.ncols, nvalid, a.back};
-  core_fft<BLUE, true, true, K1>(a.core, a.tpb, sm, ld, st);
+  CoreT::run(a.core, a.tpb, sm, ld, st);
 }
 
-}  // namespace
+}  // namespace kern
 
+#ifndef __CUDACC_RTC__
 template <typename T>
 cudaError_t launch_complex(Kernel which, bool blue, bool k1, const KArgs& a, unsigned blocks, unsigned threads,
                            size_t smem, cudaStream_t stream) {
+  using namespace kern;
   void (*fn)(const KArgs) = nullptr;
+#define CHFFT_PICK(K, TMINOR)                                                                  \
+  (blue ? (k1 ? K<T, DynCore<true, TMINOR, true, true>> : K<T, DynCore<true, TMINOR, true, false>>) \
+        : (k1 ? K<T, DynCore<false, TMINOR, true, true>> : K<T, DynCore<false, TMINOR, true, false>>))
   switch (which) {
-    case Kernel::C2C:
-      fn = blue ? (k1 ? k_c2c<T, true, true> : k_c2c<T, true, false>) : (k1 ? k_c2c<T, false, true> : k_c2c<T, false, false>);
-      break;
-    case Kernel::COLS:
-      fn = blue ? (k1 ? k_cols<T, true, true> : k_cols<T, true, false>)
-                : (k1 ? k_cols<T, false, true> : k_cols<T, false, false>);
-      break;
+    case Kernel::C2C: fn = CHFFT_PICK(k_c2c, false); break;
+    case Kernel::COLS: fn = CHFFT_PICK(k_cols, true); break;
     default: return cudaErrorInvalidValue;
   }
+#undef CHFFT_PICK
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -120,5 +117,6 @@ cudaError_t launch_complex(Kernel which, bool blue, bool k1, const KArgs& a, uns
   fn<<<blocks, threads, smem, stream>>>(a);
   return cudaGetLastError();
 }
+#endif  // __CUDACC_RTC__
 
 }  // namespace chfft

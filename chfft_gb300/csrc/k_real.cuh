@@ -8,20 +8,15 @@
 // pass's loader and post-passes that need one FFT output per result live in
 // the last pass's storer. Split steps that pair bin k with bin h-k run as a
 // separate cooperative phase on the shared-memory tile.
-// Instantiated per dtype by k_real_f32.cu / k_real_f64.cu.
+// Run-time-stage instances come from k_real_f32.cu / k_real_f64.cu, plan-time
+// specialised ones from jit.cu.
 #pragma once
 
 #include "kernels.cuh"
 
 namespace chfft {
 
-namespace {
-
-template <typename C>
-__device__ __forceinline__ C czero() {
-  using R = typename Real<C>::type;
-  return mk(R(0), R(0));
-}
+namespace kern {
 
 struct BlockRange {
   long long t0;
@@ -47,15 +42,15 @@ struct PackLoad {
   }
 };
 
-template <typename T, bool BLUE, bool K1>
-__global__ void __launch_bounds__(kMaxThreads, K1 ? 2 : 1) k_r2c(const KArgs a) {
+template <typename T, class CoreT>
+__global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_r2c(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
   const BlockRange br = block_range(a);
   const int h = a.core.n, N = 2 * h;
   PackLoad<T> ld{(const T*)a.in + br.t0 * a.in_dist, a.in_dist, br.nvalid, (T)a.scale};
-  core_fft<BLUE, false, false, K1>(a.core, a.tpb, sm, ld, sm);
+  CoreT::run(a.core, a.tpb,sm, ld, sm);
   // Split (src/rfft1d.rs:136-148): X_i = Z_i - x, X_{h-i} = Z_{h-i} + conj(x),
   // x = coef_i (Z_i - conj Z_{h-i}); DC / Nyquist / N/4 bins from item 0.
   const int qlen = (N + 3) >> 2;
@@ -93,8 +88,8 @@ struct UnpackStore {
   }
 };
 
-template <typename T, bool BLUE, bool K1>
-__global__ void __launch_bounds__(kMaxThreads, K1 ? 2 : 1) k_c2r(const KArgs a) {
+template <typename T, class CoreT>
+__global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_c2r(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
@@ -119,7 +114,7 @@ __global__ void __launch_bounds__(kMaxThreads, K1 ? 2 : 1) k_c2r(const KArgs a) 
   }
   __syncthreads();
   UnpackStore<T> st{(T*)a.out + br.t0 * a.out_dist, a.out_dist, br.nvalid, T(2.0 * a.scale)};
-  core_fft<BLUE, false, false, K1>(a.core, a.tpb, sm, sm, st);
+  CoreT::run(a.core, a.tpb,sm, sm, st);
 }
 
 // ---------------------------------------------------------------- DCT-II
@@ -145,15 +140,15 @@ struct DctPackLoad {
   }
 };
 
-template <typename T, bool BLUE, bool K1>
-__global__ void __launch_bounds__(kMaxThreads, K1 ? 2 : 1) k_dct2(const KArgs a) {
+template <typename T, class CoreT>
+__global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_dct2(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
   const BlockRange br = block_range(a);
   const int h = a.core.n, N = 2 * h;
   DctPackLoad<T> ld{(const T*)a.in + br.t0 * a.in_dist, a.in_dist, br.nvalid, N, (T)a.scale, (T)a.aux_scalar};
-  core_fft<BLUE, false, false, K1>(a.core, a.tpb, sm, ld, sm);
+  CoreT::run(a.core, a.tpb,sm, ld, sm);
   // Post-twiddle with exp(+i pi k / 2N) (src/dct1d.rs:266-289).
   const int q2 = (N + 3) >> 2;
   const C* coef = (const C*)a.aux0;
@@ -213,8 +208,8 @@ struct DctUnpackStore {
   }
 };
 
-template <typename T, bool BLUE, bool K1>
-__global__ void __launch_bounds__(kMaxThreads, K1 ? 2 : 1) k_dct3(const KArgs a) {
+template <typename T, class CoreT>
+__global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_dct3(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
@@ -243,7 +238,7 @@ __global__ void __launch_bounds__(kMaxThreads, K1 ? 2 : 1) k_dct3(const KArgs a)
   }
   __syncthreads();
   DctUnpackStore<T> st{(T*)a.out + br.t0 * a.out_dist, a.out_dist, br.nvalid, h};
-  core_fft<BLUE, false, false, K1>(a.core, a.tpb, sm, sm, st);
+  CoreT::run(a.core, a.tpb,sm, sm, st);
 }
 
 // ---------------------------------------------------------------- MDCT
@@ -302,8 +297,8 @@ struct MdctStore {
   }
 };
 
-template <typename T, bool BLUE, bool K1>
-__global__ void __launch_bounds__(kMaxThreads, K1 ? 2 : 1) k_mdct(const KArgs a) {
+template <typename T, class CoreT>
+__global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_mdct(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
@@ -312,7 +307,7 @@ __global__ void __launch_bounds__(kMaxThreads, K1 ? 2 : 1) k_mdct(const KArgs a)
   const C* tw = (const C*)a.aux0;
   MdctLoad<T> ld{(const T*)a.in + br.t0 * a.in_dist, a.in_dist, br.nvalid, n, tw, (const T*)a.aux1};
   MdctStore<T> st{(T*)a.out + br.t0 * a.out_dist, a.out_dist, br.nvalid, n >> 1, tw, (T)a.scale};
-  core_fft<BLUE, false, false, K1>(a.core, a.tpb, sm, ld, st);
+  CoreT::run(a.core, a.tpb,sm, ld, st);
 }
 
 // IMDCT: pre-twiddle x(-2) (src/mdct1d.rs:259-263), FORWARD N/4 FFT, then
@@ -360,8 +355,8 @@ struct ImdctStore {
   }
 };
 
-template <typename T, bool BLUE, bool K1>
-__global__ void __launch_bounds__(kMaxThreads, K1 ? 2 : 1) k_imdct(const KArgs a) {
+template <typename T, class CoreT>
+__global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_imdct(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
@@ -370,16 +365,20 @@ __global__ void __launch_bounds__(kMaxThreads, K1 ? 2 : 1) k_imdct(const KArgs a
   const C* tw = (const C*)a.aux0;
   ImdctLoad<T> ld{(const T*)a.in + br.t0 * a.in_dist, a.in_dist, br.nvalid, n >> 1, tw};
   ImdctStore<T> st{(T*)a.out + br.t0 * a.out_dist, a.out_dist, br.nvalid, n, tw, (const T*)a.aux1, (T)a.scale};
-  core_fft<BLUE, false, false, K1>(a.core, a.tpb, sm, ld, st);
+  CoreT::run(a.core, a.tpb,sm, ld, st);
 }
 
-}  // namespace
+}  // namespace kern
 
+#ifndef __CUDACC_RTC__
 template <typename T>
 cudaError_t launch_real(Kernel which, bool blue, bool k1, const KArgs& a, unsigned blocks, unsigned threads,
                         size_t smem, cudaStream_t stream) {
   void (*fn)(const KArgs) = nullptr;
-#define CHFFT_PICK(K) (blue ? (k1 ? K<T, true, true> : K<T, true, false>) : (k1 ? K<T, false, true> : K<T, false, false>))
+  using namespace kern;
+#define CHFFT_PICK(K)                                                                        \
+  (blue ? (k1 ? K<T, DynCore<true, false, false, true>> : K<T, DynCore<true, false, false, false>>) \
+        : (k1 ? K<T, DynCore<false, false, false, true>> : K<T, DynCore<false, false, false, false>>))
   switch (which) {
     case Kernel::R2C: fn = CHFFT_PICK(k_r2c); break;
     case Kernel::C2R: fn = CHFFT_PICK(k_c2r); break;
@@ -397,5 +396,6 @@ cudaError_t launch_real(Kernel which, bool blue, bool k1, const KArgs& a, unsign
   fn<<<blocks, threads, smem, stream>>>(a);
   return cudaGetLastError();
 }
+#endif  // __CUDACC_RTC__
 
 }  // namespace chfft

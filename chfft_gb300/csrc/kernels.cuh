@@ -2,7 +2,9 @@
 // translation units and the host plan code.
 #pragma once
 
+#ifndef __CUDACC_RTC__
 #include <cuda_runtime.h>
+#endif
 
 #include "engine.cuh"
 
@@ -41,6 +43,7 @@ enum class Kernel : int {
   IMDCT = 7,
 };
 
+#ifndef __CUDACC_RTC__
 // Launch `which` for dtype T (float or double) with `blocks` CTAs of
 // `threads` threads and `smem` bytes of dynamic shared memory; `blue`
 // selects the Bluestein core and `k1` the one-butterfly-per-thread variant.
@@ -76,5 +79,6 @@ cudaError_t gen_table(Table which, long long n, long long count, long long m, vo
 // Elementwise f64 -> T complex conversion (Bluestein spectrum rounding).
 template <typename T>
 cudaError_t convert_from_f64(const double2* src, void* dst, long long count, cudaStream_t stream);
+#endif  // __CUDACC_RTC__
 
 }  // namespace chfft

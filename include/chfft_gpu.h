@@ -165,6 +165,18 @@ CHFFT_API int chfft_swap_list(const size_t* gather, size_t n, size_t* out);
  * computed by a GPU kernel into device memory d_out (len uint64 values). */
 CHFFT_API int chfft_chirp_index_device(size_t len, uint64_t* d_out, void* stream);
 
+/* ---- plan-time kernel specialisation ------------------------------------ */
+
+/* Plans can run kernels specialised to their exact radix sequence, lengths
+ * and launch shape, compiled with NVRTC for sm_103a on first use and cached
+ * for the life of the process. CHFFT_JIT selects when: "0"/"off" never,
+ * "auto" (default) for launches of at least 2^18 elements, anything else
+ * always. Returns 1 when NVRTC and the driver API can be opened, 0 otherwise
+ * (reason in chfft_last_error; plans then use the library's kernels). */
+CHFFT_API int chfft_plan_compiler_available(void);
+/* Number of specialised kernels compiled so far in this process. */
+CHFFT_API size_t chfft_plan_compiler_cache_size(void);
+
 /* ---- diagnostics -------------------------------------------------------- */
 
 /* Message of the last failure on the calling thread ("" if none). */
