@@ -54,20 +54,28 @@ struct StageList {
   int all[kNumRadix];    // phased order: pass counts
 };
 
-// Shared-memory placement of element i of sequence t: one pad slot per 16
-// elements breaks the power-of-two strides of the early passes' writes.
-CHFFT_HD int smem_index(int t, int i, int ld) { return t * ld + i + (i >> 4); }
+// Shared-memory placement of element i of sequence t: one pad slot per P
+// elements (none for P = 0). The first pass stores with stride R (its
+// radix); P = R makes that stride R+1, which is odd for even R and so
+// conflict-free. The library kernels use P = 16.
+template <int P>
+CHFFT_HD int smem_index(int t, int i, int ld) {
+  return t * ld + i + (P > 0 ? i / (P > 0 ? P : 1) : 0);
+}
 // Odd stride: adjacent sequences then start in different banks, which keeps
 // the TMINOR (column tile) accesses conflict-free.
-CHFFT_HD int smem_ld(int n) { return (n + (n >> 4)) | 1; }
+CHFFT_HD int smem_ld(int n, int p = 16) { return (n + (p > 0 ? n / p : 0)) | 1; }
 
-template <typename C>
+template <typename C, int P = 16>
 struct SmemIO {
   C* s;
   int ld;
-  __device__ __forceinline__ C load(int t, int i) const { return s[smem_index(t, i, ld)]; }
-  __device__ __forceinline__ void store(int t, int i, C v) const { s[smem_index(t, i, ld)] = v; }
+  __device__ __forceinline__ C load(int t, int i) const { return s[smem_index<P>(t, i, ld)]; }
+  __device__ __forceinline__ void store(int t, int i, C v) const { s[smem_index<P>(t, i, ld)] = v; }
 };
+
+template <class X> struct is_tile { static constexpr bool value = false; };
+template <typename C, int P> struct is_tile<SmemIO<C, P>> { static constexpr bool value = true; };
 
 template <bool TMINOR>
 __device__ __forceinline__ void split_index(int b, int tpb, int nb, int& t, int& j) {
@@ -83,7 +91,10 @@ __device__ __forceinline__ void split_index(int b, int tpb, int nb, int& t, int&
 // One radix-R Stockham pass: ld -> registers -> butterflies -> st. Ns is the
 // product of the radices of the passes already run. All loads of the pass
 // complete (barrier) before any store, so ld and st may be the same tile.
-template <int R, bool TMINOR, bool K1, typename C, class Ld, class St>
+// Twiddles: tw is omega_n (entry r * (j mod Ns) * n / (Ns R)), or with STW
+// this pass's block of the stage table, entry (r - 1) * Ns + (j mod Ns), so
+// the r-th twiddles of a warp are one contiguous segment.
+template <int R, bool TMINOR, bool K1, bool STW = false, typename C, class Ld, class St>
 __device__ __forceinline__ void pass_body(int n, int Ns, int tpb, const C* __restrict__ tw, const Ld& ld,
                                           const St& st) {
   constexpr int K = K1 ? 1 : Ept<C>::value / R;
@@ -105,9 +116,15 @@ __device__ __forceinline__ void pass_body(int n, int Ns, int tpb, const C* __res
 #pragma unroll
       for (int r = 0; r < R; r++) v[k][r] = ld.load(t, j + r * nb);
       if (Ns > 1) {
-        const int step = (j % Ns) * tw_step;
+        if constexpr (STW) {
+          const int jm = j % Ns;
 #pragma unroll
-        for (int r = 1; r < R; r++) v[k][r] = cmul(v[k][r], __ldg(&tw[r * step]));
+          for (int r = 1; r < R; r++) v[k][r] = cmul(v[k][r], __ldg(&tw[(r - 1) * Ns + jm]));
+        } else {
+          const int step = (j % Ns) * tw_step;
+#pragma unroll
+          for (int r = 1; r < R; r++) v[k][r] = cmul(v[k][r], __ldg(&tw[r * step]));
+        }
       }
       Dft<R>::run(v[k]);
     }
@@ -215,6 +232,7 @@ struct CoreDesc {
   int n;              // logical core length
   const void* chirp;  // Bluestein: c_j, j < n
   const void* bhat;   // Bluestein: FFT_M(conj c) / M
+  const void* stw;    // stage twiddles of the fused pass order (compile-time-stage kernels)
 };
 
 // Y <- conj(Y * B^) on every sequence of the tile.
@@ -290,6 +308,12 @@ __device__ __forceinline__ void core_fft(const CoreDesc& d, int tpb, const SmemI
 template <bool BLUE, bool TMINOR, bool FUSED, bool K1>
 struct DynCore {
   static constexpr bool kK1 = K1;
+  // The kernel's shared-memory tile (layout shared with the kernel's own
+  // pre-/post-phases).
+  template <typename C>
+  __device__ __forceinline__ static SmemIO<C> tile(unsigned char* base, int ld) {
+    return SmemIO<C>{reinterpret_cast<C*>(base), ld};
+  }
   template <typename C, class Ld, class St>
   __device__ __forceinline__ static void run(const CoreDesc& d, int tpb, const SmemIO<C>& sm, const Ld& ld,
                                              const St& st) {
@@ -297,46 +321,52 @@ struct DynCore {
   }
 };
 
-// Passes R, Rest... with Ns = NS at the first: `ld` feeds the first pass,
-// `st` takes the last, the tile carries everything in between.
-template <int N, int TPB, int LD, bool TMINOR, bool K1, int NS, int R, int... Rest, typename C, class Ld, class St>
-__device__ __forceinline__ void static_passes(const C* tw, C* s, const Ld& ld, const St& st) {
+// Passes R, Rest... with Ns = NS at the first and this pass's stage-table
+// block at stw + OFF: `ld` feeds the first pass, `st` takes the last, the
+// tile carries everything in between.
+template <int N, int TPB, int LD, int P, bool TMINOR, bool K1, int NS, int OFF, int R, int... Rest, typename C,
+          class Ld, class St>
+__device__ __forceinline__ void static_passes(const C* stw, C* s, const Ld& ld, const St& st) {
   if constexpr (sizeof...(Rest) == 0) {
-    pass_body<R, TMINOR, K1>(N, NS, TPB, tw, ld, st);
+    pass_body<R, TMINOR, K1, true>(N, NS, TPB, stw + OFF, ld, st);
   } else {
-    const SmemIO<C> sm{s, LD};
-    pass_body<R, TMINOR, K1>(N, NS, TPB, tw, ld, sm);
-    static_passes<N, TPB, LD, TMINOR, K1, NS * R, Rest...>(tw, s, sm, st);
+    const SmemIO<C, P> sm{s, LD};
+    pass_body<R, TMINOR, K1, true>(N, NS, TPB, stw + OFF, ld, sm);
+    static_passes<N, TPB, LD, P, TMINOR, K1, NS * R, OFF + (R - 1) * NS, Rest...>(stw, s, sm, st);
   }
 }
 
-template <bool BLUE, bool TMINOR, bool K1, int M, int NU, int TPB, int LD, int... Rs>
+// Bluestein: the first FFT's last pass stores conj(Y_i * B^_i), the input of
+// the inverse FFT, straight into the tile.
+template <typename C, class Tile>
+struct SpectrumStore {
+  const Tile& sm;
+  const C* bhat;
+  __device__ __forceinline__ void store(int t, int i, C v) const {
+    sm.store(t, i, cconj(cmul(v, __ldg(&bhat[i]))));
+  }
+};
+
+template <bool BLUE, bool TMINOR, bool K1, int M, int NU, int TPB, int LD, int P, int... Rs>
 struct StatCore {
   static constexpr bool kK1 = K1;
+  template <typename C>
+  __device__ __forceinline__ static SmemIO<C, P> tile(unsigned char* base, int) {
+    return SmemIO<C, P>{reinterpret_cast<C*>(base), LD};
+  }
   template <typename C, class Ld, class St>
-  __device__ __forceinline__ static void run(const CoreDesc& d, int, const SmemIO<C>& sm0, const Ld& ld,
+  __device__ __forceinline__ static void run(const CoreDesc& d, int, const SmemIO<C, P>& sm, const Ld& ld,
                                              const St& st) {
-    const C* tw = static_cast<const C*>(d.tw);
-    const SmemIO<C> sm{sm0.s, LD};
-    constexpr bool kLoad = !same_type<Ld, SmemIO<C>>::value;
-    constexpr bool kStore = !same_type<St, SmemIO<C>>::value;
+    const C* stw = static_cast<const C*>(d.stw);
     if constexpr (!BLUE) {
-      if constexpr (kLoad && kStore) {
-        static_passes<M, TPB, LD, TMINOR, K1, 1, Rs...>(tw, sm.s, ld, st);
-      } else if constexpr (kLoad) {
-        static_passes<M, TPB, LD, TMINOR, K1, 1, Rs...>(tw, sm.s, ld, sm);
-      } else if constexpr (kStore) {
-        static_passes<M, TPB, LD, TMINOR, K1, 1, Rs...>(tw, sm.s, sm, st);
-      } else {
-        static_passes<M, TPB, LD, TMINOR, K1, 1, Rs...>(tw, sm.s, sm, sm);
-      }
+      static_passes<M, TPB, LD, P, TMINOR, K1, 1, 0, Rs...>(stw, sm.s, ld, st);
     } else {
       const C* chirp = static_cast<const C*>(d.chirp);
       ChirpIn<C, Ld> l1{ld, chirp, NU};
       ChirpOut<C, St> s2{st, chirp, NU};
-      static_passes<M, TPB, LD, TMINOR, K1, 1, Rs...>(tw, sm.s, l1, sm);
-      spectrum_phase<TMINOR>(sm, M, TPB, static_cast<const C*>(d.bhat));
-      static_passes<M, TPB, LD, TMINOR, K1, 1, Rs...>(tw, sm.s, sm, s2);
+      SpectrumStore<C, SmemIO<C, P>> spec{sm, static_cast<const C*>(d.bhat)};
+      static_passes<M, TPB, LD, P, TMINOR, K1, 1, 0, Rs...>(stw, sm.s, l1, spec);
+      static_passes<M, TPB, LD, P, TMINOR, K1, 1, 0, Rs...>(stw, sm.s, sm, s2);
     }
   }
 };

@@ -121,20 +121,11 @@ const char* kernel_template(Kernel k) {
   return "";
 }
 
-// Radices in the order the fused path runs them (rf, mid..., rl), or the
-// canonical order when the list has fewer than two passes.
-std::vector<int> pass_order(const StageList& st) {
-  std::vector<int> r;
-  if (st.npass >= 2) {
-    r.push_back(st.rf);
-    for (int i = 0; i < kNumRadix; i++)
-      for (int c = 0; c < st.mid[i]; c++) r.push_back(radix_at(i));
-    r.push_back(st.rl);
-  } else {
-    for (int i = 0; i < kNumRadix; i++)
-      for (int c = 0; c < st.all[i]; c++) r.push_back(radix_at(i));
-  }
-  return r;
+// Tile pad period of a specialised kernel: the first pass's radix when even
+// (its stride-R stores then become conflict-free), no padding otherwise.
+int pad_period(const StageList& st) {
+  std::vector<int> order = pass_order(st);
+  return (!order.empty() && order[0] % 2 == 0) ? order[0] : 0;
 }
 
 std::string name_expression(Kernel k, int dtype, const Core& c, const Geo& g) {
@@ -145,7 +136,8 @@ std::string name_expression(Kernel k, int dtype, const Core& c, const Geo& g) {
   s += c.blue ? "true," : "false,";
   s += k == Kernel::COLS ? "true," : "false,";
   s += g.k1 ? "true," : "false,";
-  s += std::to_string(c.st.n) + "," + std::to_string(c.n) + "," + std::to_string(g.tpb) + "," + std::to_string(g.ld);
+  s += std::to_string(c.st.n) + "," + std::to_string(c.n) + "," + std::to_string(g.tpb) + "," + std::to_string(g.ld) +
+       "," + std::to_string(pad_period(c.st));
   for (int r : pass_order(c.st)) s += "," + std::to_string(r);
   s += ">>";
   return s;
@@ -202,10 +194,18 @@ bool jit_available(std::string* why) {
   return ok;
 }
 
-int jit_launch(Kernel k, int dtype, const Core& c, const Geo& g, const KArgs& a, unsigned blocks,
+int jit_launch(Kernel k, int dtype, const Core& c, const Geo& g0, const KArgs& a0, unsigned blocks,
                cudaStream_t stream) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (!load_api()) return 1;
+  if (!c.stw.p) return 1;
+  // The specialised tile uses its own pad period, hence its own stride.
+  Geo g = g0;
+  g.ld = smem_ld(c.st.n, pad_period(c.st));
+  g.smem = (size_t)g.tpb * g.ld * cplx_bytes(dtype);
+  if (g.smem > kMaxSmem) return 1;
+  KArgs a = a0;
+  a.ld = g.ld;
   int dev = 0;
   cudaGetDevice(&dev);
   const std::string expr = name_expression(k, dtype, c, g);

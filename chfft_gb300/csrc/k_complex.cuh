@@ -45,7 +45,7 @@ template <typename T, class CoreT>
 __global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_c2c(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
+  const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
   const long long t0 = (long long)blockIdx.x * a.tpb;
   const int nvalid = (int)min((long long)a.tpb, a.count - t0);
   RowLoad<C> ld{(const C*)a.in + t0 * a.in_dist, a.in_dist, nvalid, (T)a.scale, a.back};
@@ -84,7 +84,7 @@ template <typename T, class CoreT>
 __global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_cols(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
+  const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
   const long long tr = blockIdx.x / a.tiles_per_tr;
   const int c0 = (int)(blockIdx.x - tr * a.tiles_per_tr) * a.tpb;
   const int nvalid = min(a.tpb, a.ncols - c0);

@@ -46,7 +46,7 @@ template <typename T, class CoreT>
 __global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_r2c(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
+  const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
   const BlockRange br = block_range(a);
   const int h = a.core.n, N = 2 * h;
   PackLoad<T> ld{(const T*)a.in + br.t0 * a.in_dist, a.in_dist, br.nvalid, (T)a.scale};
@@ -92,7 +92,7 @@ template <typename T, class CoreT>
 __global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_c2r(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
+  const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
   const BlockRange br = block_range(a);
   const int h = a.core.n, N = 2 * h;
   const int qlen = (N + 3) >> 2;
@@ -144,7 +144,7 @@ template <typename T, class CoreT>
 __global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_dct2(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
+  const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
   const BlockRange br = block_range(a);
   const int h = a.core.n, N = 2 * h;
   DctPackLoad<T> ld{(const T*)a.in + br.t0 * a.in_dist, a.in_dist, br.nvalid, N, (T)a.scale, (T)a.aux_scalar};
@@ -212,7 +212,7 @@ template <typename T, class CoreT>
 __global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_dct3(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
+  const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
   const BlockRange br = block_range(a);
   const int h = a.core.n, N = 2 * h;
   const int q = (N + 3) >> 2;
@@ -301,7 +301,7 @@ template <typename T, class CoreT>
 __global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_mdct(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
+  const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
   const BlockRange br = block_range(a);
   const int n = a.n_user;
   const C* tw = (const C*)a.aux0;
@@ -359,7 +359,7 @@ template <typename T, class CoreT>
 __global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_imdct(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmemIO<C> sm{reinterpret_cast<C*>(smem_raw), a.ld};
+  const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
   const BlockRange br = block_range(a);
   const int n = a.n_user;
   const C* tw = (const C*)a.aux0;

@@ -92,6 +92,26 @@ __global__ void k_gen(int which, long long n, long long count, long long m, void
 }
 
 template <typename T>
+__global__ void k_gen_stage(PassList pl, long long total, void* out) {
+  using C = cx_t<T>;
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= total) return;
+  long long off = 0, ns = 1;
+  for (int p = 0; p < pl.npass; p++) {
+    const long long r = pl.r[p], blk = (r - 1) * ns;
+    if (k < off + blk) {
+      const long long e = k - off, jm = e % ns, rr = e / ns + 1;
+      double c, s;
+      root(jm * rr, ns * r, &c, &s);
+      put<C>(out, k, c, s);
+      return;
+    }
+    off += blk;
+    ns *= r;
+  }
+}
+
+template <typename T>
 __global__ void k_from_f64(const double2* src, void* dst, long long count) {
   using C = cx_t<T>;
   using R = typename Real<C>::type;
@@ -111,6 +131,17 @@ cudaError_t gen_table(Table which, long long n, long long count, long long m, vo
 }
 
 template <typename T>
+cudaError_t gen_stage_table(const PassList& pl, void* out, cudaStream_t stream) {
+  long long total = 1;
+  for (int p = 0; p < pl.npass; p++) total *= pl.r[p];
+  total -= 1;
+  if (total <= 0) return cudaSuccess;
+  const unsigned threads = 256;
+  k_gen_stage<T><<<(unsigned)((total + threads - 1) / threads), threads, 0, stream>>>(pl, total, out);
+  return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t convert_from_f64(const double2* src, void* dst, long long count, cudaStream_t stream) {
   if (count <= 0) return cudaSuccess;
   const unsigned threads = 256;
@@ -121,6 +152,8 @@ cudaError_t convert_from_f64(const double2* src, void* dst, long long count, cud
 
 template cudaError_t gen_table<float>(Table, long long, long long, long long, void*, cudaStream_t);
 template cudaError_t gen_table<double>(Table, long long, long long, long long, void*, cudaStream_t);
+template cudaError_t gen_stage_table<float>(const PassList&, void*, cudaStream_t);
+template cudaError_t gen_stage_table<double>(const PassList&, void*, cudaStream_t);
 template cudaError_t convert_from_f64<float>(const double2*, void*, long long, cudaStream_t);
 template cudaError_t convert_from_f64<double>(const double2*, void*, long long, cudaStream_t);
 

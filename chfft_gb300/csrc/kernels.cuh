@@ -76,6 +76,17 @@ enum class Table : int {
 template <typename T>
 cudaError_t gen_table(Table which, long long n, long long count, long long m, void* out, cudaStream_t stream);
 
+// Radices of a pass order (first pass first).
+struct PassList {
+  int npass;
+  int r[24];
+};
+// Stage twiddle table of a pass order: for pass p (radix R, Ns = product of
+// the earlier radices) the block [(R-1) x Ns] holds exp(-2 pi i jm r /
+// (Ns R)) at (r-1)*Ns + jm; blocks follow pass order. prod(r) - 1 entries.
+template <typename T>
+cudaError_t gen_stage_table(const PassList& pl, void* out, cudaStream_t stream);
+
 // Elementwise f64 -> T complex conversion (Bluestein spectrum rounding).
 template <typename T>
 cudaError_t convert_from_f64(const double2* src, void* dst, long long count, cudaStream_t stream);

@@ -114,6 +114,30 @@ int threads_needed(const StageList& st, int ept, int tpb, bool k1) {
   return (int)std::min<long long>(need, INT_MAX);
 }
 
+std::vector<int> pass_order(const StageList& st) {
+  std::vector<int> r;
+  if (st.npass >= 2) {
+    r.push_back(st.rf);
+    for (int i = 0; i < kNumRadix; i++)
+      for (int c = 0; c < st.mid[i]; c++) r.push_back(radix_at(i));
+    r.push_back(st.rl);
+  } else {
+    for (int i = 0; i < kNumRadix; i++)
+      for (int c = 0; c < st.all[i]; c++) r.push_back(radix_at(i));
+  }
+  return r;
+}
+
+// Stage twiddles for the fused pass order (compile-time-stage kernels).
+static void build_stage_table(DevBuf& buf, const StageList& st, int dtype, cudaStream_t s) {
+  std::vector<int> order = pass_order(st);
+  PassList pl{};
+  pl.npass = (int)order.size();
+  for (size_t i = 0; i < order.size(); i++) pl.r[i] = order[i];
+  buf.ensure((size_t)std::max(st.n - 1, 1) * cplx_bytes(dtype));
+  CHFFT_CUDA(dtype == 0 ? gen_stage_table<float>(pl, buf.p, s) : gen_stage_table<double>(pl, buf.p, s));
+}
+
 bool fits_cta(const StageList& st, int dtype) {
   if (threads_needed(st, ept_of(dtype), 1) > kMaxThreads) return false;
   return (size_t)smem_ld(st.n) * cplx_bytes(dtype) <= kMaxSmem;
@@ -145,6 +169,7 @@ bool Core::build(long long n_, int dtype_, cudaStream_t s) {
   tw.release();
   chirp.release();
   bhat.release();
+  stw.release();
   const size_t cb = cplx_bytes(dtype);
   if (n == 1) {
     st = StageList{};
@@ -155,6 +180,7 @@ bool Core::build(long long n_, int dtype_, cudaStream_t s) {
     tw.ensure(n * cb);
     CHFFT_CUDA(dtype == 0 ? gen_table<float>(Table::OMEGA, n, n, 0, tw.p, s)
                           : gen_table<double>(Table::OMEGA, n, n, 0, tw.p, s));
+    build_stage_table(stw, st, dtype, s);
     return true;
   }
   // Bluestein core (src/chirpz.rs): chirp table and the spectrum of the
@@ -170,6 +196,7 @@ bool Core::build(long long n_, int dtype_, cudaStream_t s) {
                         : gen_table<double>(Table::OMEGA, m, m, 0, tw.p, s));
   CHFFT_CUDA(dtype == 0 ? gen_table<float>(Table::CHIRP, n, n, 0, chirp.p, s)
                         : gen_table<double>(Table::CHIRP, n, n, 0, chirp.p, s));
+  build_stage_table(stw, st, dtype, s);
   // B^ = FFT_M(b) / M in FP64 when the f64 engine can run length M in one
   // CTA; otherwise the FFT of the FP64 sequence runs in the working dtype.
   DevBuf b64;
@@ -211,6 +238,7 @@ CoreDesc Core::desc() const {
   d.n = (int)n;
   d.chirp = chirp.p;
   d.bhat = bhat.p;
+  d.stw = stw.p;
   return d;
 }
 

@@ -67,6 +67,9 @@ bool make_stages(long long n, StageList* out);
 int threads_needed(const StageList& st, int ept, int tpb, bool k1 = false);
 // Whether one sequence of these stages fits a CTA (threads and shared memory).
 bool fits_cta(const StageList& st, int dtype);
+// Radices in the order the fused kernels run them (rf, mid..., rl), or the
+// canonical order when the list has fewer than two passes.
+std::vector<int> pass_order(const StageList& st);
 
 // Complex core FFT of logical length n for one dtype: mixed radix when n is
 // 7-smooth and fits a CTA, otherwise Bluestein with a 7-smooth M >= 2n-1.
@@ -75,11 +78,11 @@ struct Core {
   int dtype = 0;
   bool blue = false;
   StageList st{};  // stages of the FFT actually run (length M for Bluestein)
-  DevBuf tw, chirp, bhat;
+  DevBuf tw, chirp, bhat, stw;
   bool build(long long n, int dtype, cudaStream_t s);  // false: unsupported size
   CoreDesc desc() const;
   long long fft_len() const { return st.n; }
-  size_t device_bytes() const { return tw.bytes + chirp.bytes + bhat.bytes; }
+  size_t device_bytes() const { return tw.bytes + chirp.bytes + bhat.bytes + stw.bytes; }
 };
 
 // Launch geometry of a CTA-per-`tpb`-sequences kernel.
