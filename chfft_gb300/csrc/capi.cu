@@ -91,6 +91,9 @@ struct PlanImpl {
   std::vector<unsigned char> custom_window;
   Core core;   // complex core (CFft1D: N; CFft2D rows: N; RFft1D/Dct1D: N/2; Mdct1D: N/4)
   Core core2;  // CFft2D columns: M
+  BigCore big;           // CFft1D beyond one CTA (four-step)
+  bool use_big = false;
+  DevBuf work;           // four-step workspace
   DevBuf aux0, aux1;
   cudaStream_t stream = nullptr;
   DevBuf stage_in, stage_out;
@@ -116,9 +119,14 @@ struct PlanImpl {
     auto need = [&](Core& c, long long n) {
       if (!c.build(n, dtype, s)) throw Fail{CHFFT_EUNSUPPORTED, "transform length " + std::to_string(n) + " exceeds the shared-memory engine"};
     };
+    use_big = false;
     switch (kind) {
       case CHFFT_KIND_CFFT1D:
-        if (len >= 2) need(core, len);
+        if (len >= 2 && !core.build(len, dtype, s)) {
+          if (!big.build(len, dtype, s))
+            throw Fail{CHFFT_EUNSUPPORTED, "transform length " + std::to_string(len) + " is not supported"};
+          use_big = true;
+        }
         break;
       case CHFFT_KIND_CFFT2D:
         if (len_m > 0 && len_n > 0) {
@@ -245,6 +253,11 @@ struct PlanImpl {
         if (len <= 1) {  // chfft returns a copy for len <= 1 (src/cfft1d.rs:212-214)
           if (d_in != d_out && len == 1)
             CHFFT_CUDA(cudaMemcpyAsync(d_out, d_in, batch * cplx_bytes(dtype), cudaMemcpyDeviceToDevice, s));
+          return;
+        }
+        if (use_big) {
+          work.ensure((size_t)big.work_elems(batch) * cplx_bytes(dtype));
+          big.exec(d_in, d_out, work.p, batch, ms.back, sc, s);
           return;
         }
         a.in_dist = a.out_dist = len;
@@ -568,9 +581,9 @@ int chfft_plan_get_info(chfft_plan plan, chfft_plan_info* info) {
   info->len = (size_t)p.len;
   info->len_m = (size_t)p.len_m;
   info->len_n = (size_t)p.len_n;
-  info->fft_len = (size_t)p.core.n;
-  info->algorithm = p.core.blue ? 1 : 0;
-  info->padded_len = p.core.blue ? (size_t)p.core.st.n : 0;
+  info->fft_len = (size_t)(p.use_big ? p.big.n : p.core.n);
+  info->algorithm = p.use_big ? (p.big.blue ? 3 : 2) : (p.core.blue ? 1 : 0);
+  info->padded_len = p.use_big ? (p.big.blue ? (size_t)p.big.m : 0) : (p.core.blue ? (size_t)p.core.st.n : 0);
   int k = 0;
   if (p.core.st.npass >= 2) {
     info->radix[k++] = p.core.st.rf;
@@ -590,7 +603,8 @@ int chfft_plan_get_info(chfft_plan plan, chfft_plan_info* info) {
   }
   info->in_elems = p.in_elems(false);
   info->out_elems = p.out_elems(false);
-  info->device_bytes = p.core.device_bytes() + p.core2.device_bytes() + p.aux0.bytes + p.aux1.bytes;
+  info->device_bytes = p.core.device_bytes() + p.core2.device_bytes() + p.big.device_bytes() + p.work.bytes +
+                       p.aux0.bytes + p.aux1.bytes;
   return CHFFT_OK;
 }
 

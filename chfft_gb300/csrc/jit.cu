@@ -117,6 +117,8 @@ const char* kernel_template(Kernel k) {
     case Kernel::DCT3: return "chfft::kern::k_dct3";
     case Kernel::MDCT: return "chfft::kern::k_mdct";
     case Kernel::IMDCT: return "chfft::kern::k_imdct";
+    case Kernel::COLS_TW: return "chfft::kern::k_cols_tw";
+    case Kernel::ROWS_T: return "chfft::kern::k_rows_t";
   }
   return "";
 }
@@ -128,18 +130,23 @@ int pad_period(const StageList& st) {
   return (!order.empty() && order[0] % 2 == 0) ? order[0] : 0;
 }
 
-std::string name_expression(Kernel k, int dtype, const Core& c, const Geo& g) {
+bool column_mapped(Kernel k) { return k == Kernel::COLS || k == Kernel::COLS_TW || k == Kernel::ROWS_T; }
+bool four_step(Kernel k) { return k == Kernel::COLS_TW || k == Kernel::ROWS_T; }
+
+std::string name_expression(Kernel k, int dtype, const Core& c, const Geo& g, int mode) {
   std::string s = "&";
   s += kernel_template(k);
   s += dtype == 0 ? "<float, " : "<double, ";
   s += "chfft::StatCore<";
   s += c.blue ? "true," : "false,";
-  s += k == Kernel::COLS ? "true," : "false,";
+  s += column_mapped(k) ? "true," : "false,";
   s += g.k1 ? "true," : "false,";
   s += std::to_string(c.st.n) + "," + std::to_string(c.n) + "," + std::to_string(g.tpb) + "," + std::to_string(g.ld) +
        "," + std::to_string(pad_period(c.st));
   for (int r : pass_order(c.st)) s += "," + std::to_string(r);
-  s += ">>";
+  s += ">";
+  if (four_step(k)) s += ", " + std::to_string(mode);
+  s += ">";
   return s;
 }
 
@@ -195,7 +202,8 @@ bool jit_available(std::string* why) {
 }
 
 int jit_launch(Kernel k, int dtype, const Core& c, const Geo& g0, const KArgs& a0, unsigned blocks,
-               cudaStream_t stream) {
+               cudaStream_t stream, int mode, const FourStep* fs) {
+  if (four_step(k) && !fs) return 1;
   std::lock_guard<std::mutex> lk(g_mu);
   if (!load_api()) return 1;
   if (!c.stw.p) return 1;
@@ -208,7 +216,7 @@ int jit_launch(Kernel k, int dtype, const Core& c, const Geo& g0, const KArgs& a
   a.ld = g.ld;
   int dev = 0;
   cudaGetDevice(&dev);
-  const std::string expr = name_expression(k, dtype, c, g);
+  const std::string expr = name_expression(k, dtype, c, g, mode);
   Entry& e = g_cache[std::to_string(dev) + "|" + expr];
   if (e.failed) return 1;
   if (!e.fn) {
@@ -223,7 +231,7 @@ int jit_launch(Kernel k, int dtype, const Core& c, const Geo& g0, const KArgs& a
     if (g_api.cuFuncSetAttribute(e.fn, kAttrMaxDynSmem, (int)g.smem) != 0) return 2;
     e.smem_set = (int)g.smem;
   }
-  void* args[] = {const_cast<KArgs*>(&a)};
+  void* args[] = {const_cast<KArgs*>(&a), const_cast<FourStep*>(fs)};
   if (g_api.cuLaunchKernel(e.fn, blocks, 1, 1, g.threads, 1, 1, (unsigned)g.smem, (CUstream)stream, args, nullptr) != 0)
     return 2;
   return 0;

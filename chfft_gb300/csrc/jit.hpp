@@ -16,7 +16,8 @@ bool jit_available(std::string* why);
 // Launch the plan-time specialised kernel for (kind, dtype, core, geometry),
 // compiling it on first use. Returns 0 on success, 1 when unavailable (the
 // caller launches the library kernel instead), 2 on a launch error.
-int jit_launch(Kernel k, int dtype, const Core& c, const Geo& g, const KArgs& a, unsigned blocks, cudaStream_t stream);
+int jit_launch(Kernel k, int dtype, const Core& c, const Geo& g, const KArgs& a, unsigned blocks, cudaStream_t stream,
+               int mode = 0, const FourStep* fs = nullptr);
 // Number of specialised kernels compiled in this process.
 size_t jit_cache_size();
 

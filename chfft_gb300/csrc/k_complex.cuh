@@ -93,9 +93,144 @@ __global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_cols(const 
   CoreT::run(a.core, a.tpb, sm, ld, st);
 }
 
+// ---------------------------------------------------------------- four-step
+// A length-N FFT with N = N1 * N2 beyond one CTA (x[n1 N2 + n2]):
+//   pass A: column FFTs of length N1, times w_N^(k1 n2), in place layout;
+//   pass B: row FFTs of length N2, written transposed to X[k1 + N1 k2].
+// The inter-pass twiddle comes from two tables: w_N^e = hi[e / L] lo[e % L]
+// (FourStep in kernels.cuh).
+
+// Pass A loader: MODE 0 plain (scale, conjugate for backward); MODE 1 the
+// Bluestein input x_j c_j for flat index j = n1 N2 + n2 < n_user, else 0.
+template <typename C, int MODE>
+struct ColsALoad {
+  const C* in;  // first column of the tile
+  int ncols, nvalid, c0;
+  typename Real<C>::type scale;
+  int back;
+  const FourStep* fs;
+  __device__ __forceinline__ C load(int t, int i) const {
+    if (t >= nvalid) return czero<C>();
+    if (MODE == 1) {
+      const long long j = (long long)i * ncols + c0 + t;
+      if (j >= fs->n_user) return czero<C>();
+      C v = cscale(in[(long long)i * ncols + t], scale);
+      if (back) v = cconj(v);
+      return cmul(v, __ldg(&static_cast<const C*>(fs->chirp)[j]));
+    }
+    C v = cscale(in[(long long)i * ncols + t], scale);
+    return back ? cconj(v) : v;
+  }
+};
+
+template <typename C>
+struct ColsAStore {
+  C* out;
+  int ncols, nvalid, c0;
+  const FourStep* fs;
+  __device__ __forceinline__ void store(int t, int k1, C v) const {
+    if (t >= nvalid) return;
+    const long long e = (long long)k1 * (c0 + t);  // < N
+    const C* lo = static_cast<const C*>(fs->lo);
+    const C* hi = static_cast<const C*>(fs->hi);
+    const C w = cmul(__ldg(&hi[e / fs->tw_l]), __ldg(&lo[e % fs->tw_l]));
+    out[(long long)k1 * ncols + t] = cmul(v, w);
+  }
+};
+
+template <typename T, class CoreT, int MODE>
+__global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_cols_tw(const KArgs a, const FourStep fs) {
+  using C = cx_t<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
+  const long long tr = blockIdx.x / a.tiles_per_tr;
+  const int c0 = (int)(blockIdx.x - tr * a.tiles_per_tr) * a.tpb;
+  const int nvalid = min(a.tpb, a.ncols - c0);
+  ColsALoad<C, MODE> ld{(const C*)a.in + tr * a.in_dist + c0, a.ncols, nvalid, c0, (T)a.scale, a.back, &fs};
+  ColsAStore<C> st{(C*)a.out + tr * a.out_dist + c0, a.ncols, nvalid, c0, &fs};
+  CoreT::run(a.core, a.tpb, sm, ld, st);
+}
+
+// Pass B storer, element k2 of row k1 goes to X[k1 + N1 k2]:
+// MODE 0 plain (conjugate for backward, the pass-A scale already applied);
+// MODE 1 Bluestein spectrum: conj(X_k B^_k), the inverse FFT's input;
+// MODE 2 Bluestein output: k < n_user gets conj(X_k) c_k (conjugated again
+// for backward).
+template <typename C, int MODE>
+struct RowsBStore {
+  C* out;  // transform base
+  int r0, nvalid, n1, back;
+  const FourStep* fs;
+  __device__ __forceinline__ void store(int t, int k2, C v) const {
+    if (t >= nvalid) return;
+    const long long k = (long long)(r0 + t) + (long long)n1 * k2;
+    if (MODE == 0) {
+      out[k] = back ? cconj(v) : v;
+    } else if (MODE == 1) {
+      out[k] = cconj(cmul(v, __ldg(&static_cast<const C*>(fs->bhat)[k])));
+    } else {
+      if (k < fs->n_user) {
+        C y = cmul(cconj(v), __ldg(&static_cast<const C*>(fs->chirp)[k]));
+        out[k] = back ? cconj(y) : y;
+      }
+    }
+  }
+};
+
+template <typename C>
+struct RowsBLoad {
+  const C* in;  // first row of the tile
+  int n2, nvalid;
+  __device__ __forceinline__ C load(int t, int i) const {
+    return t < nvalid ? in[(long long)t * n2 + i] : czero<C>();
+  }
+};
+
+template <typename T, class CoreT, int MODE>
+__global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_rows_t(const KArgs a, const FourStep fs) {
+  using C = cx_t<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
+  const long long tr = blockIdx.x / a.tiles_per_tr;
+  const int r0 = (int)(blockIdx.x - tr * a.tiles_per_tr) * a.tpb;
+  const int nvalid = min(a.tpb, fs.n1 - r0);
+  // Rows are contiguous: load them with consecutive threads along a row,
+  // then run the FFT with consecutive threads across rows so the transposed
+  // store is contiguous.
+  RowsBLoad<C> rl{(const C*)a.in + tr * a.in_dist + (long long)r0 * fs.n2, fs.n2, nvalid};
+  load_phase<false>(sm, fs.n2, a.tpb, rl);
+  RowsBStore<C, MODE> st{(C*)a.out + tr * a.out_dist, r0, nvalid, fs.n1, a.back, &fs};
+  CoreT::run(a.core, a.tpb, sm, sm, st);
+}
+
 }  // namespace kern
 
 #ifndef __CUDACC_RTC__
+template <typename T>
+cudaError_t launch_fourstep(bool pass_a, int mode, bool k1, const KArgs& a, const FourStep& fs,
+                            unsigned blocks, unsigned threads, size_t smem, cudaStream_t stream) {
+  using namespace kern;
+  void (*fn)(const KArgs, const FourStep) = nullptr;
+  if (pass_a) {
+    using K1C = DynCore<false, true, true, true>;
+    using KNC = DynCore<false, true, true, false>;
+    if (mode == 0) fn = k1 ? k_cols_tw<T, K1C, 0> : k_cols_tw<T, KNC, 0>;
+    else fn = k1 ? k_cols_tw<T, K1C, 1> : k_cols_tw<T, KNC, 1>;
+  } else {
+    using K1C = DynCore<false, true, true, true>;
+    using KNC = DynCore<false, true, true, false>;
+    if (mode == 0) fn = k1 ? k_rows_t<T, K1C, 0> : k_rows_t<T, KNC, 0>;
+    else if (mode == 1) fn = k1 ? k_rows_t<T, K1C, 1> : k_rows_t<T, KNC, 1>;
+    else fn = k1 ? k_rows_t<T, K1C, 2> : k_rows_t<T, KNC, 2>;
+  }
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  fn<<<blocks, threads, smem, stream>>>(a, fs);
+  return cudaGetLastError();
+}
+
 template <typename T>
 cudaError_t launch_complex(Kernel which, bool blue, bool k1, const KArgs& a, unsigned blocks, unsigned threads,
                            size_t smem, cudaStream_t stream) {

@@ -1,4 +1,4 @@
-// double instantiation of the complex-input kernels (k_complex.cuh).
+// double instantiation of the row / column kernels (k_complex.cuh).
 #include "k_complex.cuh"
 
 namespace chfft {

@@ -88,6 +88,10 @@ __global__ void k_gen(int which, long long n, long long count, long long m, void
       reinterpret_cast<unsigned long long*>(out)[k] =
           ((unsigned long long)k * (unsigned long long)k) % (2ull * (unsigned long long)n);
       break;
+    case Table::OMEGA_STRIDE:
+      root((long long)(((unsigned long long)k * (unsigned long long)m) % (unsigned long long)n), n, &c, &s);
+      put<C>(out, k, c, s);
+      break;
   }
 }
 

@@ -41,9 +41,29 @@ enum class Kernel : int {
   DCT3 = 5,
   MDCT = 6,
   IMDCT = 7,
+  COLS_TW = 8,  // four-step pass A
+  ROWS_T = 9,   // four-step pass B
+};
+
+// Four-step geometry of a length-N FFT beyond one CTA, N = n1 * n2.
+struct FourStep {
+  long long n;        // N
+  int n1, n2;         // rows (column-FFT length) x row length
+  int tw_l;           // L of the two-level inter-pass twiddle table
+  const void* lo;     // w_N^e, e < L
+  const void* hi;     // w_N^(e L), e < ceil(N / L)
+  long long n_user;   // Bluestein: user length (inputs past it are zero, outputs dropped)
+  const void* chirp;  // Bluestein: c_j, j < n_user
+  const void* bhat;   // Bluestein: FFT_N(conj c) / N
 };
 
 #ifndef __CUDACC_RTC__
+// Four-step passes: pass_a selects the column pass (mode 0 plain, 1 chirp
+// input) or the transposing row pass (mode 0 plain, 1 spectrum, 2 chirp output).
+template <typename T>
+cudaError_t launch_fourstep(bool pass_a, int mode, bool k1, const KArgs& a, const FourStep& fs, unsigned blocks,
+                            unsigned threads, size_t smem, cudaStream_t stream);
+
 // Launch `which` for dtype T (float or double) with `blocks` CTAs of
 // `threads` threads and `smem` bytes of dynamic shared memory; `blue`
 // selects the Bluestein core and `k1` the one-butterfly-per-thread variant.
@@ -70,7 +90,8 @@ enum class Table : int {
   SINE_WIN = 7,    // real: sin(pi (k + 1/2) / n)
   VORBIS_WIN = 8,  // real: sin(pi/2 sin^2(pi (k + 1/2) / n))
   BLUE_B = 9,      // f64 only: Bluestein kernel sequence for user length n, padded length m, x 1/m
-  CHIRP_INDEX = 10 // u64: k*k mod 2n
+  CHIRP_INDEX = 10,// u64: k*k mod 2n
+  OMEGA_STRIDE = 11 // out[k] = exp(-2 pi i (k*m mod n) / n)
 };
 
 template <typename T>

@@ -10,6 +10,10 @@
 
 #include <algorithm>
 #include <climits>
+#include <cmath>
+#include <cstdlib>
+
+#include "jit.hpp"
 
 namespace chfft {
 
@@ -301,6 +305,179 @@ Geo col_geo(const Core& c, int ncols) {
   g.threads = std::min(th, kMaxThreads);
   g.smem = (size_t)tpb * per;
   return g;
+}
+
+bool want_specialised(long long elems) {
+  const JitMode mode = jit_mode();
+  return mode == JitMode::ALWAYS || (mode == JitMode::AUTO && elems >= (1LL << 18));
+}
+
+// ---------------------------------------------------------------- four-step
+bool four_step_split(long long m, int dtype, int* n1, int* n2) {
+  const long long col_cap = dtype == 0 ? 2048 : 1024;  // column tiles of >= 8 columns
+  double best = 1e300;
+  bool ok = false;
+  for (long long d = 2; d <= col_cap && d * d <= 4 * m; d++) {
+    if (m % d) continue;
+    const long long e = m / d;
+    StageList s1, s2;
+    if (!make_stages(d, &s1) || !make_stages(e, &s2) || !fits_cta(s1, dtype) || !fits_cta(s2, dtype)) continue;
+    const double score = std::fabs(std::log((double)d) - 0.5 * std::log((double)m)) + (d > e ? 0.01 : 0.0);
+    if (score < best) {
+      best = score;
+      *n1 = (int)d;
+      *n2 = (int)e;
+      ok = true;
+    }
+  }
+  return ok;
+}
+
+static void launch_pass(bool pass_a, int mode, const Core& c, const Geo& g, const KArgs& a, const FourStep& fs,
+                        unsigned blocks, long long elems, cudaStream_t s) {
+  if (want_specialised(elems) &&
+      jit_launch(pass_a ? Kernel::COLS_TW : Kernel::ROWS_T, c.dtype, c, g, a, blocks, s, mode, &fs) == 0)
+    return;
+  CHFFT_CUDA(c.dtype == 0 ? launch_fourstep<float>(pass_a, mode, g.k1, a, fs, blocks, g.threads, g.smem, s)
+                          : launch_fourstep<double>(pass_a, mode, g.k1, a, fs, blocks, g.threads, g.smem, s));
+}
+
+bool BigCore::build(long long n_, int dtype_, cudaStream_t s) {
+  n = n_;
+  dtype = dtype_;
+  blue = false;
+  m = n;
+  const size_t cb_ = cplx_bytes(dtype);
+  if (!four_step_split(n, dtype, &n1, &n2)) {
+    // Bluestein with a four-step M >= 2n - 1 (cheapest by M * passes).
+    long long lo_m = 2 * n - 1, hi_m = 1, best_m = -1;
+    while (hi_m < lo_m) hi_m <<= 1;
+    double best = 1e300;
+    for (long long mm = lo_m; mm <= hi_m; mm++) {
+      int a1, a2;
+      if (!factor_smooth(mm).ok || !four_step_split(mm, dtype, &a1, &a2)) continue;
+      StageList s1, s2;
+      make_stages(a1, &s1);
+      make_stages(a2, &s2);
+      const double cost = (double)mm * (s1.npass + s2.npass + 1);
+      if (cost < best) {
+        best = cost;
+        best_m = mm;
+      }
+    }
+    if (best_m < 0) return false;
+    blue = true;
+    m = best_m;
+    four_step_split(m, dtype, &n1, &n2);
+  }
+  if (!ca.build(n1, dtype, s) || !cb.build(n2, dtype, s)) return false;
+  tw_l = (int)std::ceil(std::sqrt((double)m));
+  const long long nhi = (m + tw_l - 1) / tw_l;
+  lo.ensure(tw_l * cb_);
+  hi.ensure(nhi * cb_);
+  CHFFT_CUDA(dtype == 0 ? gen_table<float>(Table::OMEGA, m, tw_l, 0, lo.p, s)
+                        : gen_table<double>(Table::OMEGA, m, tw_l, 0, lo.p, s));
+  CHFFT_CUDA(dtype == 0 ? gen_table<float>(Table::OMEGA_STRIDE, m, nhi, tw_l, hi.p, s)
+                        : gen_table<double>(Table::OMEGA_STRIDE, m, nhi, tw_l, hi.p, s));
+  if (blue) {
+    chirp.ensure(n * cb_);
+    bhat.ensure(m * cb_);
+    CHFFT_CUDA(dtype == 0 ? gen_table<float>(Table::CHIRP, n, n, 0, chirp.p, s)
+                          : gen_table<double>(Table::CHIRP, n, n, 0, chirp.p, s));
+    // B^ = FFT_M(b) / M computed in FP64 by the four-step f64 engine.
+    DevBuf b64, w64;
+    b64.ensure(m * sizeof(double2));
+    CHFFT_CUDA(gen_table<double>(Table::BLUE_B, n, m, m, b64.p, s));
+    BigCore big64;
+    if (!big64.build(m, 1, s)) return false;
+    w64.ensure(big64.work_elems(1) * sizeof(double2));
+    big64.exec(b64.p, b64.p, w64.p, 1, false, 1.0, s);
+    if (dtype == 0)
+      CHFFT_CUDA(convert_from_f64<float>(static_cast<const double2*>(b64.p), bhat.p, m, s));
+    else
+      CHFFT_CUDA(cudaMemcpyAsync(bhat.p, b64.p, m * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    CHFFT_CUDA(cudaStreamSynchronize(s));
+  }
+  return true;
+}
+
+FourStep BigCore::fs() const {
+  FourStep f{};
+  f.n = m;
+  f.n1 = n1;
+  f.n2 = n2;
+  f.tw_l = tw_l;
+  f.lo = lo.p;
+  f.hi = hi.p;
+  f.n_user = n;
+  f.chirp = chirp.p;
+  f.bhat = bhat.p;
+  return f;
+}
+
+long long BigCore::chunk(long long batch) const {
+  long long budget_mb = 64;
+  if (const char* e = std::getenv("CHFFT_L2_BUDGET_MB")) budget_mb = std::max(1LL, std::atoll(e));
+  const long long per = m * (long long)cplx_bytes(dtype) * (blue ? 2 : 1);
+  return std::max(1LL, std::min(batch, (budget_mb << 20) / per));
+}
+
+long long BigCore::work_elems(long long batch) const { return chunk(batch) * m * (blue ? 2 : 1); }
+
+void BigCore::exec(const void* in, void* out, void* work, long long batch, bool back, double scale,
+                   cudaStream_t s) const {
+  const size_t cb_ = cplx_bytes(dtype);
+  const long long g = chunk(batch);
+  char* tmp = static_cast<char*>(work);
+  char* tmp2 = tmp + g * m * cb_;
+  const FourStep f = fs();
+  const Geo ga = col_geo(ca, n2), gb = col_geo(cb, n1);
+  for (long long c0 = 0; c0 < batch; c0 += g) {
+    const long long cnt = std::min(g, batch - c0);
+    const char* src = static_cast<const char*>(in) + c0 * n * cb_;
+    char* dst = static_cast<char*>(out) + c0 * n * cb_;
+    auto pass_a = [&](int mode, const void* i, long long idist, void* o, double sc, int bk) {
+      KArgs a{};
+      a.core = ca.desc();
+      a.tpb = ga.tpb;
+      a.ld = ga.ld;
+      a.back = bk;
+      a.count = cnt;
+      a.tiles_per_tr = (n2 + ga.tpb - 1) / ga.tpb;
+      a.in = i;
+      a.out = o;
+      a.scale = sc;
+      a.in_dist = idist;
+      a.out_dist = m;
+      a.ncols = n2;
+      launch_pass(true, mode, ca, ga, a, f, (unsigned)(cnt * a.tiles_per_tr), cnt * m, s);
+    };
+    auto pass_b = [&](int mode, const void* i, void* o, long long odist, int bk) {
+      KArgs a{};
+      a.core = cb.desc();
+      a.tpb = gb.tpb;
+      a.ld = gb.ld;
+      a.back = bk;
+      a.count = cnt;
+      a.tiles_per_tr = (n1 + gb.tpb - 1) / gb.tpb;
+      a.in = i;
+      a.out = o;
+      a.scale = 1.0;
+      a.in_dist = m;
+      a.out_dist = odist;
+      a.ncols = n2;
+      launch_pass(false, mode, cb, gb, a, f, (unsigned)(cnt * a.tiles_per_tr), cnt * m, s);
+    };
+    if (!blue) {
+      pass_a(0, src, n, tmp, scale, back);
+      pass_b(0, tmp, dst, n, back);
+    } else {
+      pass_a(1, src, n, tmp, scale, back);  // x c, zero padded
+      pass_b(1, tmp, tmp2, m, 0);           // conj(X B^)
+      pass_a(0, tmp2, m, tmp, 1.0, 0);      // inverse FFT as a conjugated forward FFT
+      pass_b(2, tmp, dst, n, back);         // conj(.) c, k < n
+    }
+  }
 }
 
 }  // namespace chfft

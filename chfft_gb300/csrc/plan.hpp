@@ -98,4 +98,33 @@ Geo col_geo(const Core& c, int ncols);
 // Smallest 7-smooth M >= lo that the CTA engine runs cheapest (M * passes).
 long long bluestein_length(long long n, int dtype);
 
+// Whether plan-time specialised kernels are used for a launch of `elems`
+// elements (CHFFT_JIT policy).
+bool want_specialised(long long elems);
+
+// Complex FFT of a length beyond one CTA: four-step N = n1 * n2 (column
+// pass + transposing row pass, jit/library kernels), or Bluestein with a
+// four-step M. The batch runs in chunks sized to keep the intermediate in L2.
+struct BigCore {
+  long long n = 0;  // logical length
+  long long m = 0;  // FFT length run (n, or the Bluestein M)
+  int dtype = 0;
+  bool blue = false;
+  int n1 = 0, n2 = 0, tw_l = 0;
+  Core ca, cb;  // column core (n1), row core (n2)
+  DevBuf lo, hi, chirp, bhat;
+  bool build(long long n, int dtype, cudaStream_t s);  // false: unsupported
+  FourStep fs() const;
+  long long chunk(long long batch) const;                  // transforms per chunk
+  long long work_elems(long long batch) const;             // complex workspace elements
+  // batch contiguous sequences in -> out (distance n), workspace `work`.
+  void exec(const void* in, void* out, void* work, long long batch, bool back, double scale, cudaStream_t s) const;
+  size_t device_bytes() const {
+    return ca.device_bytes() + cb.device_bytes() + lo.bytes + hi.bytes + chirp.bytes + bhat.bytes;
+  }
+};
+
+// Split of a 7-smooth m into n1 x n2 CTA-sized factors (false if none).
+bool four_step_split(long long m, int dtype, int* n1, int* n2);
+
 }  // namespace chfft

@@ -265,3 +265,36 @@ def test_config_cfft2d_2048_f32():
     p = cg.CFft2D.with_len(2048, 2048, np.float32)
     y = p.forward(x)
     assert rel(y, np.fft.fft2(x.astype(np.complex128))) <= 5e-6
+
+
+# ---------------------------------------------------------------- beyond one CTA (four-step)
+@pytest.mark.parametrize("n,dt", [(32768, np.float32), (65536, np.float32), (1 << 20, np.float32), (16384, np.float64),
+                                  (3 * 5 * 7 * 2 ** 9, np.float32), (65521, np.float32), (20011, np.float64)])
+def test_cfft1d_four_step(n, dt):
+    """Lengths beyond one CTA: four-step (7-smooth) or four-step Bluestein (primes)."""
+    rng = np.random.default_rng(n)
+    x = (rng.standard_normal((3, n)) + 1j * rng.standard_normal((3, n))).astype(CPLX[dt])
+    p = cg.CFft1D.with_len(n, dt)
+    info = p.info()
+    assert info.algorithm in (2, 3)
+    ref = np.fft.fft(x.astype(np.complex128), axis=-1)
+    tol = 1e-11 if dt == np.float64 else 5e-6
+    for meth, r in (("forward", ref), ("forwardn", ref / n)):
+        assert rel(p.execute_batch(meth, x), r) <= tol
+    y = p.execute_batch("forward", x)
+    assert rel(p.execute_batch("backward", y), x) <= tol
+    assert rel(p.forward(x[0]), ref[0]) <= tol
+
+
+def test_config_1m_x64_f32():
+    """N = 2^20 x 64 f32, N(0,1) with 1% of entries x 1e3: rel-L2 against FP64."""
+    n, b = 1 << 20, 64
+    rng = np.random.default_rng(4)
+    x = (rng.standard_normal((b, n), dtype=np.float32) + 1j * rng.standard_normal((b, n), dtype=np.float32))
+    spikes = rng.random((b, n)) < 0.01
+    x[spikes] *= 1e3
+    x = x.astype(np.complex64)
+    p = cg.CFft1D.with_len(n, np.float32)
+    y = p.execute_batch("forward", x)
+    for i in (0, 31, 63):
+        assert rel(y[i], np.fft.fft(x[i].astype(np.complex128))) <= 1e-6
