@@ -746,3 +746,26 @@ int chfft_plan_compiler_available(void) {
 size_t chfft_plan_compiler_cache_size(void) { return chfft::jit_cache_size(); }
 
 }  // extern "C"
+
+namespace chfft {
+
+// Sets the message chfft_last_error returns on this thread (noalloc.cu).
+int record_error(int code, const std::string& msg) { return set_error(code, msg); }
+
+// For the no-allocation entry point (noalloc.cu): the four-step core of a
+// CFft1D plan and the direction / scale of `method`. Returns a status and
+// sets the last error when the plan does not run on the four-step path.
+int plan_four_step(chfft_plan plan, int method, const BigCore** big, bool* back, double* scale) {
+  if (!plan) return set_error(CHFFT_EINVAL, "null plan");
+  const PlanImpl& p = plan->impl;
+  if (p.kind != CHFFT_KIND_CFFT1D || !p.use_big)
+    return set_error(CHFFT_EINVAL, "the no-allocation entry point runs CFft1D plans on the four-step path only");
+  MethodSpec ms = method_spec(p.kind, method);
+  if (!ms.ok) return set_error(CHFFT_EINVAL, "method not offered by this type");
+  *big = &p.big;
+  *back = ms.back;
+  *scale = p.scale_value(ms.scale);
+  return CHFFT_OK;
+}
+
+}  // namespace chfft

@@ -334,8 +334,8 @@ bool four_step_split(long long m, int dtype, int* n1, int* n2) {
 }
 
 static void launch_pass(bool pass_a, int mode, const Core& c, const Geo& g, const KArgs& a, const FourStep& fs,
-                        unsigned blocks, long long elems, cudaStream_t s) {
-  if (want_specialised(elems) &&
+                        unsigned blocks, long long elems, cudaStream_t s, bool library_only = false) {
+  if (!library_only && want_specialised(elems) &&
       jit_launch(pass_a ? Kernel::COLS_TW : Kernel::ROWS_T, c.dtype, c, g, a, blocks, s, mode, &fs) == 0)
     return;
   CHFFT_CUDA(c.dtype == 0 ? launch_fourstep<float>(pass_a, mode, g.k1, a, fs, blocks, g.threads, g.smem, s)
@@ -425,9 +425,9 @@ long long BigCore::chunk(long long batch) const {
 long long BigCore::work_elems(long long batch) const { return chunk(batch) * m * (blue ? 2 : 1); }
 
 void BigCore::exec(const void* in, void* out, void* work, long long batch, bool back, double scale,
-                   cudaStream_t s) const {
+                   cudaStream_t s, long long max_chunk, bool library_only) const {
   const size_t cb_ = cplx_bytes(dtype);
-  const long long g = chunk(batch);
+  const long long g = max_chunk > 0 ? std::min(chunk(batch), max_chunk) : chunk(batch);
   char* tmp = static_cast<char*>(work);
   char* tmp2 = tmp + g * m * cb_;
   const FourStep f = fs();
@@ -450,7 +450,7 @@ void BigCore::exec(const void* in, void* out, void* work, long long batch, bool 
       a.in_dist = idist;
       a.out_dist = m;
       a.ncols = n2;
-      launch_pass(true, mode, ca, ga, a, f, (unsigned)(cnt * a.tiles_per_tr), cnt * m, s);
+      launch_pass(true, mode, ca, ga, a, f, (unsigned)(cnt * a.tiles_per_tr), cnt * m, s, library_only);
     };
     auto pass_b = [&](int mode, const void* i, void* o, long long odist, int bk) {
       KArgs a{};
@@ -466,7 +466,7 @@ void BigCore::exec(const void* in, void* out, void* work, long long batch, bool 
       a.in_dist = m;
       a.out_dist = odist;
       a.ncols = n2;
-      launch_pass(false, mode, cb, gb, a, f, (unsigned)(cnt * a.tiles_per_tr), cnt * m, s);
+      launch_pass(false, mode, cb, gb, a, f, (unsigned)(cnt * a.tiles_per_tr), cnt * m, s, library_only);
     };
     if (!blue) {
       pass_a(0, src, n, tmp, scale, back);

@@ -118,7 +118,12 @@ struct BigCore {
   long long chunk(long long batch) const;                  // transforms per chunk
   long long work_elems(long long batch) const;             // complex workspace elements
   // batch contiguous sequences in -> out (distance n), workspace `work`.
-  void exec(const void* in, void* out, void* work, long long batch, bool back, double scale, cudaStream_t s) const;
+  // max_chunk > 0 caps the transforms per chunk (a fixed-size workspace);
+  // library_only skips plan-time specialised kernels.
+  void exec(const void* in, void* out, void* work, long long batch, bool back, double scale, cudaStream_t s,
+            long long max_chunk = 0, bool library_only = false) const;
+  // Workspace bytes one transform needs.
+  size_t work_bytes_per_transform() const { return (size_t)m * cplx_bytes(dtype) * (blue ? 2 : 1); }
   size_t device_bytes() const {
     return ca.device_bytes() + cb.device_bytes() + lo.bytes + hi.bytes + chirp.bytes + bhat.bytes;
   }

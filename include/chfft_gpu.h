@@ -131,6 +131,35 @@ CHFFT_API int chfft_execute_batch(chfft_plan plan, int method, const void* src, 
 CHFFT_API int chfft_execute_device(chfft_plan plan, int method, const void* d_src, void* d_dst, size_t batch,
                                    void* stream);
 
+/* Device execution that allocates nothing. No counterpart in the reference
+ * (chfft allocates a new Vec for every result).
+ *
+ * For callers that cannot allocate device memory when they run a transform:
+ * code running while a stream is captured into a CUDA graph, real-time loops
+ * that must not wait on the allocator, hosts whose device memory belongs to a
+ * pool they do not control. chfft_execute_device grows the plan's workspace
+ * with cudaMalloc on a large batch; this variant runs CFft1D plans on the
+ * four-step path (lengths beyond one CTA, see chfft_plan_info.algorithm 2/3)
+ * with the workspace taken from a fixed array of CHFFT_NOALLOC_SCRATCH_BYTES
+ * that the library defines per device and every GPU that loads the library
+ * holds until the process exits. It calls no cudaMalloc/cudaFree and no
+ * allocating library routine; it always uses the library's own kernels
+ * (never the plan-time compiler). Inputs and outputs are the caller's device
+ * buffers, as for chfft_execute_device.
+ *
+ * Limits and rules: one transform's workspace (8 or 16 bytes x the FFT
+ * length, twice that for Bluestein lengths) must fit the array, else the call
+ * returns CHFFT_EUNSUPPORTED with the sizes in chfft_last_error; larger
+ * batches run in chunks that fit. The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture. All calls share the array
+ * and it keeps the last call's contents (nothing in it needs to start at
+ * zero), so calls whose work overlaps on the GPU (different streams, no
+ * ordering) race on it. Other plans get CHFFT_EINVAL. */
+#define CHFFT_NOALLOC_SCRATCH_BYTES (16u << 20)
+CHFFT_API int chfft_execute_device_noalloc(chfft_plan plan, int method, const void* d_src, void* d_dst, size_t batch,
+                                           void* stream);
+
 /* ---- plan inspection ---------------------------------------------------- */
 
 typedef struct chfft_plan_info {
