@@ -142,6 +142,24 @@ def profiled_traffic():
     return out
 
 
+# ---------------------------------------------------------------------------- ranks
+def reduce_max(values, world, device=None):
+    """Element-wise max of per-rank timings over the process group (replicas:
+    every rank runs the full workload on its own GPU, no data exchange)."""
+    if world <= 1:
+        return list(values)
+    import torch
+
+    t = torch.tensor(list(values), dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return [float(v) for v in t.cpu()]
+
+
+def aggregate_value(world, seconds):
+    """Whole-job GFLOP/s: every rank's work over the slowest rank's time."""
+    return world * TOTAL_FLOPS / seconds / 1e9
+
+
 # ---------------------------------------------------------------------------- CPU
 def cpu_run(steps: int, warmup: int, threads: int):
     """The oracle (chfft's algorithm, C++) on the full workload; seconds per step."""
@@ -268,10 +286,7 @@ def run_gpu(args, rank, world, local_rank):
     clk = clocks.stop()
     e2e_s = statistics.mean(e2e_times)
 
-    if world > 1:
-        t = torch.tensor([ms, e2e_s], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms, e2e_s = float(t[0]), float(t[1])
+    ms, e2e_s = reduce_max([ms, e2e_s], world, device=dev)
     if rank != 0:
         return 0
 
@@ -296,7 +311,7 @@ def run_gpu(args, rank, world, local_rank):
     traffic = profiled_traffic().get(dname)
     h2d = sum(int(h.numel() * 4) for h in h_in)
     d2h = sum(int(h.numel() * 4) for h in h_out)
-    value = world * TOTAL_FLOPS / (ms * 1e-3) / 1e9
+    value = aggregate_value(world, ms * 1e-3)
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
@@ -308,7 +323,7 @@ def run_gpu(args, rank, world, local_rank):
         "roofline": {"bound": "hbm", "kernel": dname, "achieved": round(achieved, 1), "peak": peak,
                      "peak_source": f"{peak_src} hbm_gbs", "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "traffic": traffic, "algorithmic_bytes": dom_bytes},
-        "e2e": {"value": round(world * TOTAL_FLOPS / e2e_s / 1e9, 2), "unit": "GFLOP/s", "h2d_bytes_per_step": h2d,
+        "e2e": {"value": round(aggregate_value(world, e2e_s), 2), "unit": "GFLOP/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_s * 1e3, 3)},
         "gpu_launches": 4 * args.steps,
         "clocks": clk,
