@@ -464,6 +464,87 @@ class Mdct1D(_Plan):
     def backwardu(self, source): return self._host("backwardu", source, self._len)
 
 
+# ---- uneven batches ----------------------------------------------------------
+
+class BatchJob(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("method", ctypes.c_int), ("len", ctypes.c_size_t),
+                ("in_offset", ctypes.c_size_t), ("out_offset", ctypes.c_size_t), ("option", ctypes.c_int)]
+
+
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("jobs", ctypes.c_size_t), ("tasks", ctypes.c_size_t), ("ctas", ctypes.c_uint),
+                ("smem_per_cta", ctypes.c_size_t), ("workspace_bytes", ctypes.c_size_t),
+                ("four_step_lengths", ctypes.c_size_t), ("one_cta_lengths", ctypes.c_size_t)]
+
+
+KINDS = {"cfft1d": KIND_CFFT1D, "rfft1d": KIND_RFFT1D, "dct1d": KIND_DCT1D, "mdct1d": KIND_MDCT1D}
+
+
+def job_bytes(kind: str, n: int):
+    """(input bytes, output bytes) of one f32 forward job."""
+    if kind == "cfft1d":
+        return 8 * n, 8 * n
+    if kind == "rfft1d":
+        return 4 * n, 8 * (n // 2 + 1)
+    if kind == "dct1d":
+        return 4 * n, 4 * n
+    return 4 * n, 2 * n  # mdct1d: n reals -> n/2 reals
+
+
+def pack_jobs(specs, align: int = 16):
+    """specs: [(kind, n, method, option)] -> (jobs array, input bytes, output bytes, offsets)."""
+    jobs = (BatchJob * len(specs))()
+    ib = ob = 0
+    offs = []
+    for i, (kind, n, method, option) in enumerate(specs):
+        bi, bo = job_bytes(kind, n)
+        jobs[i] = BatchJob(KINDS[kind], METHODS[method], n, ib, ob, option)
+        offs.append((ib, ob))
+        ib += (bi + align - 1) // align * align
+        ob += (bo + align - 1) // align * align
+    return jobs, ib, ob, offs
+
+
+class Batch:
+    """Uneven batch: many f32 forward transforms in one persistent launch."""
+
+    def __init__(self, specs, dtype=np.float32):
+        L = lib()
+        for name, args in {
+            "chfft_batch_create": [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)],
+            "chfft_batch_execute": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+            "chfft_batch_execute_graph": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+            "chfft_batch_wait": [ctypes.c_void_p, ctypes.c_void_p],
+            "chfft_batch_get_info": [ctypes.c_void_p, ctypes.POINTER(BatchInfo)],
+            "chfft_batch_destroy": [ctypes.c_void_p],
+        }.items():
+            getattr(L, name).argtypes = args
+            getattr(L, name).restype = ctypes.c_int
+        self.specs = list(specs)
+        self.jobs, self.in_bytes, self.out_bytes, self.offsets = pack_jobs(self.specs)
+        self._h = ctypes.c_void_p()
+        _check(L.chfft_batch_create(_dtype_id(dtype), ctypes.cast(self.jobs, ctypes.c_void_p), len(self.specs),
+                                    ctypes.byref(self._h)))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.chfft_batch_destroy(h)
+            self._h = None
+
+    def info(self) -> BatchInfo:
+        out = BatchInfo()
+        _check(lib().chfft_batch_get_info(self._h, ctypes.byref(out)))
+        return out
+
+    def execute(self, d_in: int, d_out: int, stream: int = 0, graph: bool = False):
+        fn = lib().chfft_batch_execute_graph if graph else lib().chfft_batch_execute
+        _check(fn(self._h, ctypes.c_void_p(d_in), ctypes.c_void_p(d_out), ctypes.c_void_p(stream)))
+
+    def wait(self, stream: int = 0):
+        _check(lib().chfft_batch_wait(self._h, ctypes.c_void_p(stream)))
+
+
 # ---- index arithmetic (bit-exact with the reference's plan code) -----------
 
 def factorize(len: int, max_prime: int = 7):

@@ -1,0 +1,291 @@
+// Persistent uneven-batch kernel (see k_batch.cuh). f32 only.
+//
+// Every task runs the same three steps: a kind-specific load phase into the
+// shared-memory tile, the complex core on the tile (one call site for every
+// task type, so the pass code is instantiated once), and a kind-specific
+// store phase. Real-kind pre- and post-processing follow chfft's formulas
+// (src/rfft1d.rs:128-148, src/dct1d.rs:248-289, src/mdct1d.rs:206-241).
+#include "k_batch.cuh"
+
+namespace chfft {
+namespace {
+
+using C = float2;
+
+__device__ __forceinline__ C ldcg(const C* p) { return __ldcg(p); }
+
+// DCT-II input reorder v = (x0, x2, ..., x_{N-2}, x_{N-1}, ..., x3, x1).
+__device__ __forceinline__ float dct_v(const float* x, int n, int j) {
+  return j < (n >> 1) ? x[2 * j] : x[2 * (n - 1 - j) + 1];
+}
+
+// z_i of a real kind's complex core input (i < ncore), scaled.
+__device__ __forceinline__ C real_pre(const BatchItem& it, const char* in_base, long long i) {
+  const float* x = reinterpret_cast<const float*>(in_base + it.in_off);
+  if (it.kind == BK_R2C) return mk(x[2 * i] * it.scale, x[2 * i + 1] * it.scale);
+  if (it.kind == BK_DCT2) {
+    float re = dct_v(x, it.n, (int)(2 * i)), im = dct_v(x, it.n, (int)(2 * i + 1));
+    if (i == 0) re *= it.ortho;
+    return mk(re * it.scale, im * it.scale);
+  }
+  // MDCT: window, fold and pre-twiddle
+  const float* w = static_cast<const float*>(it.aux1);
+  const C* tw = static_cast<const C*>(it.aux0);
+  const int lenh = it.n >> 1, lenq = lenh >> 1, leno = lenq - (lenq >> 1), len3q = lenh + lenq, len5q = lenh + len3q;
+  const int k = (int)(i << 1);
+  float re, im;
+  if (i < leno) {
+    re = x[len3q - 1 - k] * w[len3q - 1 - k] + x[len3q + k] * w[len3q + k];
+    im = x[lenq + k] * w[lenq + k] - x[lenq - 1 - k] * w[lenq - 1 - k];
+  } else {
+    re = x[len3q - 1 - k] * w[len3q - 1 - k] - x[k - lenq] * w[k - lenq];
+    im = x[lenq + k] * w[lenq + k] + x[len5q - 1 - k] * w[len5q - 1 - k];
+  }
+  return cmul(mk(re, im), __ldg(&tw[i]));
+}
+
+// R2C split (src/rfft1d.rs:136-148) / DCT-II post-twiddle (src/dct1d.rs:266-289)
+// for pair index i of one transform; zk(k) returns core output Z_k.
+template <class Z>
+__device__ __forceinline__ void real_post(const BatchItem& it, char* out_base, int i, const Z& zk) {
+  const int h = it.ncore, N = it.n;
+  if (it.kind == BK_R2C) {
+    C* o = reinterpret_cast<C*>(out_base + it.out_off);
+    const int qlen = (N + 3) >> 2;
+    if (i >= qlen) return;
+    if (i == 0) {
+      C z0 = zk(0);
+      o[0] = mk(z0.x + z0.y, 0.f);
+      o[h] = mk(z0.x - z0.y, 0.f);
+      if ((N & 3) == 0) o[qlen] = cconj(zk(qlen));
+    } else {
+      C zi = zk(i), zh = zk(h - i);
+      C x = cmul(__ldg(&static_cast<const C*>(it.aux0)[i]), csub(zi, cconj(zh)));
+      o[i] = csub(zi, x);
+      o[h - i] = cadd(zh, cconj(x));
+    }
+    return;
+  }
+  float* o = reinterpret_cast<float*>(out_base + it.out_off);
+  const C* coef = static_cast<const C*>(it.aux0);
+  const C* om = static_cast<const C*>(it.aux1);
+  const int q2 = (N + 3) >> 2;
+  if (i >= q2) return;
+  if (i == 0) {
+    C z0 = zk(0);
+    o[0] = z0.x + z0.y;
+    o[h] = (z0.x - z0.y) * __ldg(&om[h]).x;
+    if ((N & 3) == 0) {
+      C x = cmul(zk(q2), __ldg(&om[q2]));
+      o[q2] = x.x;
+      o[N - q2] = x.y;
+    }
+  } else {
+    C zi = zk(i);
+    C wconj = cconj(zk(h - i));
+    C x = cmul(__ldg(&coef[i]), csub(zi, wconj));
+    C j = cmul(cconj(csub(zi, x)), __ldg(&om[i]));
+    o[i] = j.x;
+    o[N - i] = j.y;
+    C k = cmul(cadd(wconj, x), __ldg(&om[h - i]));
+    o[h - i] = k.x;
+    o[h + i] = k.y;
+  }
+}
+
+__device__ __forceinline__ void wait_for(const BatchArgs& A, int ctr, int target) {
+  if (threadIdx.x == 0) {
+    volatile int* c = A.ctr + ctr;
+    int it = 0;
+    while (*c < target) {
+      if (++it > A.spin_limit) {
+        atomicExch(A.err, 1);
+        break;
+      }
+      __nanosleep(200);
+    }
+    __threadfence();
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ void signal(const BatchArgs& A, int ctr) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(A.ctr + ctr, 1);
+  }
+}
+
+__global__ void __launch_bounds__(kBatchThreads) k_batch(const BatchArgs A) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* sbase = reinterpret_cast<C*>(smem_raw);
+  __shared__ int s_task;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_task = atomicAdd(A.next, 1);
+    __syncthreads();
+    const int ti = s_task;
+    if (ti >= A.ntasks) return;
+    const BatchTask tk = A.tasks[ti];
+    if (tk.wait_ctr >= 0) wait_for(A, tk.wait_ctr, tk.wait_target);
+    const BatchItem& it = A.items[tk.item];
+    const int tid = threadIdx.x, nth = blockDim.x;
+
+    if (tk.type == BT_POST) {
+      const C* z = reinterpret_cast<const C*>(A.work + it.work2_off);
+      const int i = tk.tile * kPostChunk;
+      for (int p = i + tid; p < i + kPostChunk; p += nth) real_post(it, A.out, p, [&](int k) { return ldcg(z + k); });
+      if (tk.signal_ctr >= 0) signal(A, tk.signal_ctr);
+      continue;
+    }
+
+    // ---- the core and its tile
+    const BatchCore& core = tk.type == BT_SMALL ? it.core : (tk.type == BT_FS_A ? it.ca : it.cb);
+    const int m = core.st.n;
+    const int tpb = tk.type == BT_SMALL ? tk.count : kBatchTile;
+    const SmemIO<C> sm{sbase, smem_ld(m)};
+    const FourStep& fs = it.fs;
+
+    // ---- load phase
+    if (tk.type == BT_SMALL) {
+      for (int b = tid; b < tpb * m; b += nth) {
+        const int t = b / m, i = b - t * m;
+        const BatchItem& x = A.items[tk.item + t];
+        C v = czero<C>();
+        if (i < core.n) {
+          if (x.kind == BK_C2C)
+            v = cscale(reinterpret_cast<const C*>(A.in + x.in_off)[i], x.scale);
+          else
+            v = real_pre(x, A.in, i);
+          if (core.blue) v = cmul(v, __ldg(&static_cast<const C*>(core.chirp)[i]));
+        }
+        sm.store(t, i, v);
+      }
+    } else if (tk.type == BT_FS_A) {
+      const int c0 = tk.tile * kBatchTile;
+      for (int b = tid; b < tpb * m; b += nth) {
+        const int t = b % kBatchTile, i = b / kBatchTile;  // consecutive threads: adjacent columns
+        const int col = c0 + t;
+        C v = czero<C>();
+        if (col < fs.n2) {
+          const long long flat = (long long)i * fs.n2 + col;
+          if (tk.mode == 2) {
+            v = ldcg(reinterpret_cast<const C*>(A.work + it.work2_off) + flat);
+          } else if (it.kind == BK_C2C) {
+            if (tk.mode == 0 || flat < fs.n_user) {
+              v = cscale(reinterpret_cast<const C*>(A.in + it.in_off)[flat], it.scale);
+              if (tk.mode == 1) v = cmul(v, __ldg(&static_cast<const C*>(fs.chirp)[flat]));
+            }
+          } else {
+            v = real_pre(it, A.in, flat);
+          }
+        }
+        sm.store(t, i, v);
+      }
+    } else {  // BT_FS_B
+      const int r0 = tk.tile * kBatchTile;
+      const C* w = reinterpret_cast<const C*>(A.work + it.work_off);
+      for (int b = tid; b < tpb * m; b += nth) {
+        const int t = b / m, i = b - t * m;  // consecutive threads along a row
+        const int row = r0 + t;
+        sm.store(t, i, row < fs.n1 ? ldcg(w + (long long)row * fs.n2 + i) : czero<C>());
+      }
+    }
+    __syncthreads();
+
+    // ---- complex core (one call site for every task type)
+    const int rounds = core.blue ? 2 : 1;
+    for (int r = 0; r < rounds; r++) {
+      if (r == 1) spectrum_phase<false>(sm, m, tpb, static_cast<const C*>(core.bhat));
+      smem_passes<false, false>(core.st.all, m, 1, tpb, static_cast<const C*>(core.tw), sm);
+    }
+
+    // ---- store phase
+    if (tk.type == BT_SMALL) {
+      const int L = core.n;
+      if (core.blue) {  // Z_k = conj(Y_k) c_k, in place
+        for (int b = tid; b < tpb * L; b += nth) {
+          const int t = b / L, k = b - t * L;
+          sm.store(t, k, cmul(cconj(sm.load(t, k)), __ldg(&static_cast<const C*>(core.chirp)[k])));
+        }
+        __syncthreads();
+      }
+      if (it.kind == BK_C2C || it.kind == BK_MDCT) {
+        for (int b = tid; b < tpb * L; b += nth) {
+          const int t = b / L, k = b - t * L;
+          const BatchItem& x = A.items[tk.item + t];
+          const C z = sm.load(t, k);
+          if (x.kind == BK_C2C) {
+            reinterpret_cast<C*>(A.out + x.out_off)[k] = z;
+          } else {
+            C r = cmul(z, cscale(__ldg(&static_cast<const C*>(x.aux0)[k]), x.scale));
+            float* o = reinterpret_cast<float*>(A.out + x.out_off);
+            o[2 * k] = -r.x;
+            o[(x.n >> 1) - 1 - 2 * k] = r.y;
+          }
+        }
+      } else {
+        const int pairs = (it.n + 3) >> 2;
+        for (int b = tid; b < tpb * pairs; b += nth) {
+          const int t = b / pairs, i = b - t * pairs;
+          real_post(A.items[tk.item + t], A.out, i, [&](int k) { return sm.load(t, k); });
+        }
+      }
+    } else if (tk.type == BT_FS_A) {
+      const int c0 = tk.tile * kBatchTile;
+      C* w = reinterpret_cast<C*>(A.work + it.work_off);
+      const C* lo = static_cast<const C*>(fs.lo);
+      const C* hi = static_cast<const C*>(fs.hi);
+      for (int b = tid; b < tpb * m; b += nth) {
+        const int t = b % kBatchTile, k1 = b / kBatchTile;
+        const int col = c0 + t;
+        if (col >= fs.n2) continue;
+        const long long e = (long long)k1 * col;
+        const C tw = cmul(__ldg(&hi[e / fs.tw_l]), __ldg(&lo[e % fs.tw_l]));
+        w[(long long)k1 * fs.n2 + col] = cmul(sm.load(t, k1), tw);
+      }
+    } else {  // BT_FS_B: X[k1 + n1 k2]
+      const int r0 = tk.tile * kBatchTile;
+      for (int b = tid; b < tpb * m; b += nth) {
+        const int t = b % kBatchTile, k2 = b / kBatchTile;  // consecutive threads: adjacent k1
+        const int row = r0 + t;
+        if (row >= fs.n1) continue;
+        const long long k = row + (long long)fs.n1 * k2;
+        const C v = sm.load(t, k2);
+        if (tk.mode == 0) {
+          reinterpret_cast<C*>(A.out + it.out_off)[k] = v;
+        } else if (tk.mode == 1) {
+          reinterpret_cast<C*>(A.work + it.work2_off)[k] = cconj(cmul(v, __ldg(&static_cast<const C*>(fs.bhat)[k])));
+        } else if (tk.mode == 2) {
+          if (k < fs.n_user)
+            reinterpret_cast<C*>(A.out + it.out_off)[k] =
+                cmul(cconj(v), __ldg(&static_cast<const C*>(fs.chirp)[k]));
+        } else {
+          reinterpret_cast<C*>(A.work + it.work2_off)[k] = v;
+        }
+      }
+    }
+    if (tk.signal_ctr >= 0) signal(A, tk.signal_ctr);
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_batch(const BatchArgs& a, unsigned blocks, size_t smem, cudaStream_t stream) {
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  k_batch<<<blocks, kBatchThreads, smem, stream>>>(a);
+  return cudaGetLastError();
+}
+
+int batch_blocks_per_sm(size_t smem) {
+  int n = 0;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch, kBatchThreads, smem) != cudaSuccess) return 1;
+  return n > 0 ? n : 1;
+}
+
+}  // namespace chfft

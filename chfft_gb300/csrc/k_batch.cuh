@@ -1,0 +1,81 @@
+// Persistent uneven-batch kernel: one launch runs a whole list of tasks of
+// mixed kinds and lengths, taken in order from a device work queue.
+//
+// Task types
+//   SMALL  `count` consecutive transforms of one kind and length, whole in
+//          one CTA (C2C, R2C, DCT-II, MDCT; mixed radix or Bluestein core)
+//   FS_A   four-step column tile: 16 columns of length n1, pre-processing of
+//          the kind fused into the load, w_m^(k1 n2) into the store
+//   FS_B   four-step row tile: 16 rows of length n2, transposed store (plain,
+//          Bluestein spectrum, Bluestein chirp-out, or the core output of a
+//          real kind for its POST tasks)
+//   POST   the R2C split / DCT-II post-twiddle of a four-step real kind
+// Dependencies are device counters: a task waits (bounded spin, thread 0)
+// until its counter reaches the number of tiles of the step it consumes,
+// and signals its own counter when done. Tasks are queued level by level, so
+// a waited-for task is always held by a CTA that is already running.
+// Workspace written by other CTAs is read with L1-bypassing loads.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace chfft {
+
+constexpr int kBatchThreads = 256;
+constexpr int kBatchTile = 16;  // four-step tile width (columns / rows)
+
+enum BatchKind : int { BK_C2C = 0, BK_R2C = 1, BK_DCT2 = 2, BK_MDCT = 3 };
+enum BatchTaskType : int { BT_SMALL = 0, BT_FS_A = 1, BT_FS_B = 2, BT_POST = 3 };
+
+struct BatchCore {
+  StageList st;       // stages run (length M for Bluestein)
+  const void* tw;     // omega_{st.n}
+  const void* chirp;  // Bluestein
+  const void* bhat;   // Bluestein
+  int n;              // logical length
+  int blue;
+};
+
+struct BatchItem {
+  int kind;             // BatchKind
+  int n;                // user length
+  int ncore;            // complex core length (n, n/2, n/4)
+  int big;              // 0 one CTA, 1 four-step, 2 four-step Bluestein
+  float scale;
+  float ortho;          // DCT-II first-input factor
+  long long in_off;     // bytes from the input base
+  long long out_off;    // bytes from the output base
+  long long work_off;   // bytes from the workspace base (big items)
+  long long work2_off;
+  BatchCore core;       // one-CTA items
+  BatchCore ca, cb;     // big items: column (n1) and row (n2) cores
+  FourStep fs;          // big items
+  const void* aux0;     // kind tables (coef, omega_4N, MDCT twiddle)
+  const void* aux1;     // (omega_4N, window)
+};
+
+struct BatchTask {
+  int type;         // BatchTaskType
+  int item;         // first item
+  int count;        // SMALL: consecutive items of the same kind / length
+  int mode;         // FS_A: 0 plain, 1 chirp in; FS_B: 0 out, 1 spectrum, 2 chirp out, 3 core out (real kinds)
+  int tile;         // FS_A / FS_B tile, POST chunk
+  int wait_ctr, wait_target, signal_ctr;
+};
+
+struct BatchArgs {
+  const BatchTask* tasks;
+  int ntasks;
+  const BatchItem* items;
+  int* next;          // queue head
+  int* ctr;           // dependency counters
+  int* err;           // error word (1: a wait gave up)
+  const char* in;
+  char* out;
+  char* work;
+  int spin_limit;     // wait iterations before giving up
+};
+
+constexpr int kPostChunk = 2048;  // pairs per POST task
+
+}  // namespace chfft

@@ -160,6 +160,48 @@ CHFFT_API int chfft_execute_device(chfft_plan plan, int method, const void* d_sr
 CHFFT_API int chfft_execute_device_noalloc(chfft_plan plan, int method, const void* d_src, void* d_dst, size_t batch,
                                            void* stream);
 
+/* ---- uneven batches ------------------------------------------------------ */
+
+/* Many transforms of mixed kinds and lengths in one persistent launch fed by
+ * a device work queue. No counterpart in the reference (one chfft call is one
+ * transform); each job means the reference call `plan.method(&src)` of its
+ * kind at its length. Jobs are f32 forward methods of CFft1D, RFft1D, Dct1D
+ * (DCT-II) and Mdct1D; lengths from 2 up to 2^18 (C2C) and a 7-smooth half
+ * length for real kinds beyond 8192. Lengths beyond one CTA run as four-step
+ * task chains synchronised by device counters (bounded waits). */
+typedef struct chfft_batch_job {
+  int kind;          /* CHFFT_KIND_CFFT1D, _RFFT1D, _DCT1D (type II), _MDCT1D */
+  int method;        /* a forward method of the kind (CHFFT_FORWARD, ...) */
+  size_t len;        /* the plan length (the reference's `len`) */
+  size_t in_offset;  /* bytes from the input base to this job's input */
+  size_t out_offset; /* bytes from the output base to this job's output */
+  int option;        /* Dct1D: is_ortho; Mdct1D: CHFFT_WINDOW_SINE or _VORBIS */
+} chfft_batch_job;
+
+typedef struct chfft_batch_s* chfft_batch;
+
+typedef struct chfft_batch_info {
+  size_t jobs, tasks;
+  unsigned ctas;              /* persistent CTAs per launch */
+  size_t smem_per_cta;
+  size_t workspace_bytes;     /* four-step intermediates */
+  size_t four_step_lengths, one_cta_lengths;
+} chfft_batch_info;
+
+/* Builds every table and the task queue (device memory). */
+CHFFT_API int chfft_batch_create(int dtype, const chfft_batch_job* jobs, size_t njobs, chfft_batch* out);
+/* One persistent launch on `stream`: d_in / d_out are the bases the job
+ * offsets refer to. Asynchronous. */
+CHFFT_API int chfft_batch_execute(chfft_batch batch, const void* d_in, void* d_out, void* stream);
+/* The same launch captured once into a CUDA graph (re-captured when the base
+ * pointers change) and replayed on `stream`. */
+CHFFT_API int chfft_batch_execute_graph(chfft_batch batch, const void* d_in, void* d_out, void* stream);
+/* Waits for `stream`; CHFFT_ETIMEOUT if a task gave up waiting for its
+ * dependencies (the launch then returned without hanging). */
+CHFFT_API int chfft_batch_wait(chfft_batch batch, void* stream);
+CHFFT_API int chfft_batch_get_info(chfft_batch batch, chfft_batch_info* info);
+CHFFT_API int chfft_batch_destroy(chfft_batch batch);
+
 /* ---- plan inspection ---------------------------------------------------- */
 
 typedef struct chfft_plan_info {
