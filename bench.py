@@ -340,6 +340,277 @@ def run_gpu(args, rank, world, local_rank):
     return 0
 
 
+# ---------------------------------------------------------------------------- other configurations
+# Optional workloads (--workload): the other BASELINE configurations, measured
+# the same way; the default workload above is the headline line.
+
+def smooth_numbers(lo, hi, primes=(2, 3, 5)):
+    out = {1}
+    for p in primes:
+        grow = set(out)
+        for v in out:
+            x = v
+            while x * p <= hi:
+                x *= p
+                grow.add(x)
+        out = grow
+    return np.array(sorted(v for v in out if v >= lo))
+
+
+def primes_upto(n):
+    s = np.ones(n + 1, bool)
+    s[:2] = False
+    for i in range(2, int(n ** 0.5) + 1):
+        if s[i]:
+            s[i * i::i] = False
+    return np.nonzero(s)[0]
+
+
+def uneven_specs(count=10000, seed=4):
+    """10,000 jobs, lengths log-uniform in [16, 65536]; C2C 60 % (a quarter of
+    them prime, so ~15 % of all jobs), RFft1D 20 %, DCT-II 10 % (even
+    {2,3,5}-smooth lengths), MDCT 10 % (frame 2048, sine window)."""
+    rng = np.random.default_rng(seed)
+    sm = smooth_numbers(16, 65536)
+    even = sm[sm % 2 == 0]
+    pr = primes_upto(65536)
+    pr = pr[pr >= 16]
+    specs = []
+    for _ in range(count):
+        u = rng.random()
+        kind = "cfft1d" if u < 0.6 else "rfft1d" if u < 0.8 else "dct1d" if u < 0.9 else "mdct1d"
+        x = math.exp(rng.uniform(math.log(16), math.log(65536)))
+        if kind == "mdct1d":
+            n = 2048
+        elif kind == "cfft1d" and rng.random() < 0.25:
+            n = int(pr[np.argmin(np.abs(pr - x))])
+        elif kind == "cfft1d":
+            n = int(sm[np.argmin(np.abs(sm - x))])
+        else:
+            n = int(even[np.argmin(np.abs(even - x))])
+        specs.append((kind, n, "forward", 0))
+    return specs
+
+
+def spec_flops(kind, n):
+    return (5.0 if kind == "cfft1d" else 2.5) * n * math.log2(n)
+
+
+def spec_bytes(kind, n):
+    return {"cfft1d": 16 * n, "rfft1d": 4 * n + 8 * (n // 2 + 1), "dct1d": 8 * n, "mdct1d": 6 * n}[kind]
+
+
+def time_events(fn, steps, warmup, flush, stream):
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    evs = []
+    for _ in range(steps):
+        if flush is not None:
+            flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        evs.append((a, b))
+    torch.cuda.synchronize()
+    return statistics.mean(a.elapsed_time(b) for a, b in evs)
+
+
+def oracle_job(spec, x):
+    import oracle
+
+    kind, n, method, _ = spec
+    if kind == "cfft1d":
+        return oracle.cfft1d(x, method, timing=True)[1]
+    if kind == "rfft1d":
+        return oracle.rfft1d(x, method, timing=True)[1]
+    if kind == "dct1d":
+        return oracle.dct1d(x, 2, False, method, timing=True)[1]
+    return oracle.mdct1d(x, n, "sine", method, timing=True)[1]
+
+
+def run_uneven(args):
+    import concurrent.futures as cf
+
+    import torch
+
+    import chfft_gb300 as cg
+
+    specs = uneven_specs()
+    b = cg.Batch(specs)
+    rng = np.random.default_rng(5)
+    host_in = torch.empty(b.in_bytes, dtype=torch.uint8).pin_memory()
+    raw = rng.uniform(-1, 1, b.in_bytes // 4).astype(np.float32)
+    host_in.numpy()[:] = raw.view(np.uint8)
+    host_out = torch.empty(b.out_bytes, dtype=torch.uint8).pin_memory()
+    d_in = host_in.cuda()
+    d_out = torch.empty(b.out_bytes, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    run = lambda: b.execute(d_in.data_ptr(), d_out.data_ptr(), sptr, graph=True)  # noqa: E731
+    run()
+    b.wait(sptr)
+    # spot-check 200 jobs against the oracle
+    out = d_out.cpu().numpy()
+    import oracle  # noqa: F401
+
+    chk = np.random.default_rng(6).choice(len(specs), 200, replace=False)
+    worst = 0.0
+    for i in chk:
+        kind, n, method, _ = specs[i]
+        io, oo = b.offsets[i]
+        bi, bo = cg.job_bytes(kind, n)
+        xin = host_in.numpy()[io:io + bi]
+        x = xin.view(np.complex64).astype(np.complex128) if kind == "cfft1d" else xin.view(np.float32).astype(np.float64)
+        y = out[oo:oo + bo].view(np.complex64 if kind in ("cfft1d", "rfft1d") else np.float32)
+        if kind == "cfft1d":
+            ref = np.fft.fft(x)
+        elif kind == "rfft1d":
+            ref = np.fft.rfft(x)
+        elif kind == "dct1d":
+            ref = oracle.dct1d(x, 2)
+        else:
+            ref = oracle.mdct1d(x, n, "sine")
+        worst = max(worst, float(np.linalg.norm(y - ref) / np.linalg.norm(ref)))
+    if worst > 5e-6:
+        raise SystemExit(f"uneven batch: worst rel-L2 {worst:.2e}")
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    clocks = ClockSampler(0).start()
+    ms = time_events(run, args.steps, args.warmup, flush, stream)
+
+    def e2e():
+        d_in.copy_(host_in, non_blocking=True)
+        run()
+        host_out.copy_(d_out, non_blocking=True)
+        stream.synchronize()
+
+    for _ in range(args.warmup):
+        e2e()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    clk = clocks.stop()
+    flops = sum(spec_flops(k, n) for k, n, _, _ in specs)
+    nbytes = sum(spec_bytes(k, n) for k, n, _, _ in specs)
+    info = b.info()
+    line = {
+        "metric": METRIC, "value": round(flops / (ms * 1e-3) / 1e9, 2), "unit": "GFLOP/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uniform[-1,1))",
+        "config": {"workload": "uneven batch: 10000 jobs, lengths log-uniform [16, 65536], 60% C2C (15% of all prime), "
+                               "20% RFft1D, 10% DCT-II, 10% MDCT 2048 sine; one persistent launch in a CUDA graph",
+                   "l2": "flushed between timed steps", "tasks": info.tasks, "ctas": info.ctas,
+                   "four_step_lengths": info.four_step_lengths, "one_cta_lengths": info.one_cta_lengths},
+        "hbm_gbs": round(nbytes / (ms * 1e-3) / 1e9, 1),
+        "roofline": {"bound": "hbm", "kernel": "k_batch", "achieved": round(nbytes / (ms * 1e-3) / 1e9, 1),
+                     "peak": 6767.1, "unit": "GB/s", "frac": round(nbytes / (ms * 1e-3) / 1e9 / 6767.1, 4),
+                     "traffic": None, "algorithmic_bytes": nbytes},
+        "e2e": {"value": round(flops / e2e_s / 1e9, 2), "unit": "GFLOP/s", "h2d_bytes_per_step": b.in_bytes,
+                "d2h_bytes_per_step": b.out_bytes, "ms_per_step": round(e2e_s * 1e3, 3)},
+        "gpu_launches": args.steps, "max_rel_l2_checked": worst, "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        sample = [int(i) for i in np.random.default_rng(7).choice(len(specs), 1000, replace=False)]
+
+        def one(i):
+            kind, n, _, _ = specs[i]
+            io, _ = b.offsets[i]
+            bi, _ = cg.job_bytes(kind, n)
+            xin = host_in.numpy()[io:io + bi]
+            x = xin.view(np.complex64) if kind == "cfft1d" else xin.view(np.float32)
+            return oracle_job(specs[i], x.copy())
+
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(threads) as ex:
+            list(ex.map(one, sample))
+        wall = time.perf_counter() - t0
+        sflops = sum(spec_flops(specs[i][0], specs[i][1]) for i in sample)
+        line["cpu_baseline"] = {"value": round(sflops / wall / 1e9, 3), "unit": "GFLOP/s", "cores": threads,
+                                "kind": "port", "sample": "1000 of the 10000 jobs, one oracle call per job over all "
+                                                           "host threads"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_large(args):
+    import torch
+
+    import chfft_gb300 as cg
+
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+    parts = [("c2c_2^20x64", 1 << 20, 64), ("c2c_16384x4096", 16384, 4096)]
+    rng = np.random.default_rng(4)
+    plans, d_in, d_out, h_in, h_out = [], [], [], [], []
+    worst = 0.0
+    for name, n, batch in parts:
+        x = rng.standard_normal((batch, n), dtype=np.float32) + 1j * rng.standard_normal((batch, n), dtype=np.float32)
+        spikes = rng.random((batch, n)) < 0.01
+        x[spikes] *= 1e3
+        x = x.astype(np.complex64)
+        p = cg.CFft1D.with_len(n, np.float32)
+        plans.append(p)
+        t = torch.from_numpy(x.view(np.float32)).to(dev)
+        d_in.append(t)
+        d_out.append(torch.empty_like(t))
+        h_in.append(torch.from_numpy(x.view(np.float32)).pin_memory())
+        h_out.append(torch.empty_like(h_in[-1]).pin_memory())
+        p.execute_device("forward", t.data_ptr(), d_out[-1].data_ptr(), batch, sptr)
+        torch.cuda.synchronize()
+        y = d_out[-1].cpu().numpy().view(np.complex64)
+        for i in (0, batch - 1):
+            ref = np.fft.fft(x[i].astype(np.complex128))
+            worst = max(worst, float(np.linalg.norm(y[i] - ref) / np.linalg.norm(ref)))
+        del x
+    if worst > 1e-6:
+        raise SystemExit(f"large workload: rel-L2 {worst:.2e} > 1e-6")
+    clocks = ClockSampler(0).start()
+    part_ms = []
+    for i, (name, n, batch) in enumerate(parts):
+        part_ms.append(time_events(lambda: plans[i].execute_device("forward", d_in[i].data_ptr(), d_out[i].data_ptr(),
+                                                                    batch, sptr), args.steps, args.warmup, None, stream))
+    e2e_t = []
+    for i, (name, n, batch) in enumerate(parts):
+        for k in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            rc = cg.lib().chfft_execute_batch(plans[i].handle, cg.METHODS["forward"], h_in[i].data_ptr(),
+                                              h_out[i].data_ptr(), batch)
+            if rc:
+                raise SystemExit(cg.lib().chfft_last_error().decode())
+            if k >= args.warmup:
+                e2e_t.append((i, time.perf_counter() - t0))
+    clk = clocks.stop()
+    e2e_s = sum(statistics.mean(t for j, t in e2e_t if j == i) for i in range(len(parts)))
+    flops = sum(5.0 * n * math.log2(n) * b for _, n, b in parts)
+    nbytes = sum(16.0 * n * b for _, n, b in parts)
+    ms = sum(part_ms)
+    line = {
+        "metric": METRIC, "value": round(flops / (ms * 1e-3) / 1e9, 2), "unit": "GFLOP/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic N(0,1) complex with 1% of entries x1e3 (seeded)",
+        "config": {"workload": "cfft1d f32 2^20 x 64 + cfft1d f32 16384 x 4096, forward, plain FP32 path",
+                   "l2": "inputs larger than L2 (512 MiB per part)"},
+        "hbm_gbs": round(nbytes / (ms * 1e-3) / 1e9, 1),
+        "parts": {name: {"ms": round(t, 4), "gbs": round(16.0 * n * b / (t * 1e-3) / 1e9, 1),
+                         "frac_of_measured_hbm": round(16.0 * n * b / (t * 1e-3) / 1e9 / 6767.1, 4)}
+                  for (name, n, b), t in zip(parts, part_ms)},
+        "max_rel_l2_vs_fp64": worst,
+        "e2e": {"value": round(flops / e2e_s / 1e9, 2), "unit": "GFLOP/s",
+                "h2d_bytes_per_step": int(nbytes / 2), "d2h_bytes_per_step": int(nbytes / 2),
+                "ms_per_step": round(e2e_s * 1e3, 3)},
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -347,6 +618,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["batch", "large", "uneven"], default="batch",
+                    help="batch: the headline configuration (default); large / uneven: the other configurations")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -354,6 +627,10 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.workload == "uneven":
+        return run_uneven(args)
+    if args.workload == "large":
+        return run_large(args)
     if world > 1:
         import torch
 

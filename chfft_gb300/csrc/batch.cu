@@ -30,11 +30,11 @@ int batch_blocks_per_sm(size_t smem);
 
 namespace {
 
-constexpr size_t kBatchSmemCap = 100 * 1024;  // per CTA: two CTAs of 256 threads per SM
+constexpr size_t kBatchSmemCap = 100 * 1024;  // per CTA: two CTAs of 512 threads per SM
 constexpr int kMaxSplit = 512;                // four-step factors in the batch kernel
 
 bool batch_fits(const StageList& st, int tpb) {
-  return threads_needed(st, 32, tpb) <= kBatchThreads && (size_t)tpb * smem_ld(st.n) * 8 <= kBatchSmemCap;
+  return threads_needed(st, kBatchEpt, tpb) <= kBatchThreads && (size_t)tpb * smem_ld(st.n) * 8 <= kBatchSmemCap;
 }
 
 // Tables of one complex core as the batch kernel runs it.
@@ -405,7 +405,7 @@ int chfft_batch_create(int dtype, const chfft_batch_job* jobs, size_t njobs, chf
       while (j < js.size() && !items[j].big && js[j].kind == js[i].kind && js[j].n == js[i].n && js[j].opt == js[i].opt)
         j++;
       const StageList& st = items[i].core.st;
-      int tpb = std::max(1, kBatchThreads / std::max(1, threads_needed(st, 32, 1)));
+      int tpb = std::max(1, kBatchThreads / std::max(1, threads_needed(st, kBatchEpt, 1)));
       while (tpb > 1 && !batch_fits(st, tpb)) tpb--;
       for (size_t k = i; k < j; k += tpb) {
         const int cnt = (int)std::min<size_t>(tpb, j - k);

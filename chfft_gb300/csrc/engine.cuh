@@ -94,10 +94,11 @@ __device__ __forceinline__ void split_index(int b, int tpb, int nb, int& t, int&
 // Twiddles: tw is omega_n (entry r * (j mod Ns) * n / (Ns R)), or with STW
 // this pass's block of the stage table, entry (r - 1) * Ns + (j mod Ns), so
 // the r-th twiddles of a warp are one contiguous segment.
-template <int R, bool TMINOR, bool K1, bool STW = false, typename C, class Ld, class St>
+// EPT > 0 overrides the per-thread element budget of the non-K1 variant.
+template <int R, bool TMINOR, bool K1, bool STW = false, int EPT = 0, typename C, class Ld, class St>
 __device__ __forceinline__ void pass_body(int n, int Ns, int tpb, const C* __restrict__ tw, const Ld& ld,
                                           const St& st) {
-  constexpr int K = K1 ? 1 : Ept<C>::value / R;
+  constexpr int K = K1 ? 1 : (EPT > 0 ? EPT : Ept<C>::value) / R;
   const int nb = n / R;
   const int total = tpb * nb;
   const int tw_step = (Ns > 1) ? n / (Ns * R) : 0;
@@ -161,16 +162,16 @@ __device__ __forceinline__ void pass_any(int R, int n, int Ns, int tpb, const C*
 
 // cnt[i] passes of radix radix_at(i) on the tile, in canonical order.
 // Returns the updated radix product Ns.
-template <bool TMINOR, bool K1, typename C>
+template <bool TMINOR, bool K1, int EPT = 0, typename C>
 __device__ __forceinline__ int smem_passes(const int* cnt, int n, int Ns, int tpb, const C* tw, const SmemIO<C>& sm) {
-  for (int c = 0; c < cnt[0]; c++, Ns *= 16) pass_body<16, TMINOR, K1>(n,Ns, tpb, tw, sm, sm);
-  for (int c = 0; c < cnt[1]; c++, Ns *= 8) pass_body<8, TMINOR, K1>(n,Ns, tpb, tw, sm, sm);
-  for (int c = 0; c < cnt[2]; c++, Ns *= 4) pass_body<4, TMINOR, K1>(n,Ns, tpb, tw, sm, sm);
-  for (int c = 0; c < cnt[3]; c++, Ns *= 2) pass_body<2, TMINOR, K1>(n,Ns, tpb, tw, sm, sm);
-  for (int c = 0; c < cnt[4]; c++, Ns *= 10) pass_body<10, TMINOR, K1>(n,Ns, tpb, tw, sm, sm);
-  for (int c = 0; c < cnt[5]; c++, Ns *= 5) pass_body<5, TMINOR, K1>(n,Ns, tpb, tw, sm, sm);
-  for (int c = 0; c < cnt[6]; c++, Ns *= 3) pass_body<3, TMINOR, K1>(n,Ns, tpb, tw, sm, sm);
-  for (int c = 0; c < cnt[7]; c++, Ns *= 7) pass_body<7, TMINOR, K1>(n,Ns, tpb, tw, sm, sm);
+  for (int c = 0; c < cnt[0]; c++, Ns *= 16) pass_body<16, TMINOR, K1, false, EPT>(n, Ns, tpb, tw, sm, sm);
+  for (int c = 0; c < cnt[1]; c++, Ns *= 8) pass_body<8, TMINOR, K1, false, EPT>(n, Ns, tpb, tw, sm, sm);
+  for (int c = 0; c < cnt[2]; c++, Ns *= 4) pass_body<4, TMINOR, K1, false, EPT>(n, Ns, tpb, tw, sm, sm);
+  for (int c = 0; c < cnt[3]; c++, Ns *= 2) pass_body<2, TMINOR, K1, false, EPT>(n, Ns, tpb, tw, sm, sm);
+  for (int c = 0; c < cnt[4]; c++, Ns *= 10) pass_body<10, TMINOR, K1, false, EPT>(n, Ns, tpb, tw, sm, sm);
+  for (int c = 0; c < cnt[5]; c++, Ns *= 5) pass_body<5, TMINOR, K1, false, EPT>(n, Ns, tpb, tw, sm, sm);
+  for (int c = 0; c < cnt[6]; c++, Ns *= 3) pass_body<3, TMINOR, K1, false, EPT>(n, Ns, tpb, tw, sm, sm);
+  for (int c = 0; c < cnt[7]; c++, Ns *= 7) pass_body<7, TMINOR, K1, false, EPT>(n, Ns, tpb, tw, sm, sm);
   return Ns;
 }
 

@@ -117,7 +117,7 @@ __device__ __forceinline__ void signal(const BatchArgs& A, int ctr) {
   }
 }
 
-__global__ void __launch_bounds__(kBatchThreads) k_batch(const BatchArgs A) {
+__global__ void __launch_bounds__(kBatchThreads, 2) k_batch(const BatchArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* sbase = reinterpret_cast<C*>(smem_raw);
   __shared__ int s_task;
@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const BatchArgs A) {
     const int rounds = core.blue ? 2 : 1;
     for (int r = 0; r < rounds; r++) {
       if (r == 1) spectrum_phase<false>(sm, m, tpb, static_cast<const C*>(core.bhat));
-      smem_passes<false, false>(core.st.all, m, 1, tpb, static_cast<const C*>(core.tw), sm);
+      smem_passes<false, false, kBatchEpt>(core.st.all, m, 1, tpb, static_cast<const C*>(core.tw), sm);
     }
 
     // ---- store phase

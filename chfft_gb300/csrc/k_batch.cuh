@@ -21,7 +21,8 @@
 
 namespace chfft {
 
-constexpr int kBatchThreads = 256;
+constexpr int kBatchThreads = 512;
+constexpr int kBatchEpt = 16;   // complex elements per thread per pass (64 registers)
 constexpr int kBatchTile = 16;  // four-step tile width (columns / rows)
 
 enum BatchKind : int { BK_C2C = 0, BK_R2C = 1, BK_DCT2 = 2, BK_MDCT = 3 };
