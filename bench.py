@@ -545,7 +545,7 @@ def run_large(args):
     dev = torch.device("cuda", 0)
     stream = torch.cuda.current_stream(dev)
     sptr = stream.cuda_stream
-    parts = [("c2c_2^20x64", 1 << 20, 64), ("c2c_16384x4096", 16384, 4096)]
+    parts = [("c2c_2^20x64", 1 << 20, 64), ("c2c_4096x16384", 4096, 16384)]
     rng = np.random.default_rng(4)
     plans, d_in, d_out, h_in, h_out = [], [], [], [], []
     worst = 0.0
@@ -575,6 +575,35 @@ def run_large(args):
     for i, (name, n, batch) in enumerate(parts):
         part_ms.append(time_events(lambda: plans[i].execute_device("forward", d_in[i].data_ptr(), d_out[i].data_ptr(),
                                                                     batch, sptr), args.steps, args.warmup, None, stream))
+    # The tensor-core form: radix-16 passes as FP16 / BF16 split-operand
+    # matrix products with FP32 accumulation, same plans, same inputs.
+    from chfft_gb300 import tuning
+
+    tc_parts = {}
+    for i, (name, n, batch) in enumerate(parts):
+        row = {"fp32": {"ms": round(part_ms[i], 4), "rel_l2": None}}
+        for prec, label in ((0, "fp32"), (1, "tc_fp16x2"), (2, "tc_bf16x2"), (3, "tc_bf16x3")):
+            cfg = tuning.default_config()
+            cfg.tc_precision = prec
+            tuning.set_config(plans[i], cfg)
+            fn = lambda: plans[i].execute_device("forward", d_in[i].data_ptr(), d_out[i].data_ptr(), batch, sptr)  # noqa: E731
+            try:
+                fn()
+            except Exception as e:  # noqa: BLE001
+                row[label] = {"unavailable": str(e)}
+                continue
+            torch.cuda.synchronize()
+            err = 0.0
+            xs = h_in[i].numpy().view(np.complex64)
+            ys = d_out[i].cpu().numpy().view(np.complex64)
+            for r in (0, batch - 1):
+                ref = np.fft.fft(xs[r].astype(np.complex128))
+                err = max(err, float(np.linalg.norm(ys[r] - ref) / np.linalg.norm(ref)))
+            ms = part_ms[i] if prec == 0 else time_events(fn, args.steps, args.warmup, None, stream)
+            row[label] = {"ms": round(ms, 4), "rel_l2_vs_fp64": err,
+                          "speedup_vs_fp32": round(part_ms[i] / ms, 3)}
+        tuning.set_config(plans[i], tuning.default_config())
+        tc_parts[name] = row
     e2e_t = []
     for i, (name, n, batch) in enumerate(parts):
         for k in range(args.warmup + args.steps):
@@ -595,17 +624,79 @@ def run_large(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic N(0,1) complex with 1% of entries x1e3 (seeded)",
-        "config": {"workload": "cfft1d f32 2^20 x 64 + cfft1d f32 16384 x 4096, forward, plain FP32 path",
+        "config": {"workload": "cfft1d f32 N=2^20 x 64 + cfft1d f32 N=4096 x 16384, forward, plain FP32 path",
                    "l2": "inputs larger than L2 (512 MiB per part)"},
         "hbm_gbs": round(nbytes / (ms * 1e-3) / 1e9, 1),
         "parts": {name: {"ms": round(t, 4), "gbs": round(16.0 * n * b / (t * 1e-3) / 1e9, 1),
                          "frac_of_measured_hbm": round(16.0 * n * b / (t * 1e-3) / 1e9 / 6767.1, 4)}
                   for (name, n, b), t in zip(parts, part_ms)},
         "max_rel_l2_vs_fp64": worst,
+        "tensor_core_form": tc_parts,
         "e2e": {"value": round(flops / e2e_s / 1e9, 2), "unit": "GFLOP/s",
                 "h2d_bytes_per_step": int(nbytes / 2), "d2h_bytes_per_step": int(nbytes / 2),
                 "ms_per_step": round(e2e_s * 1e3, 3)},
         "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_costmodel(args):
+    """Learned plan cost model: exhaustive autotune timings of seeded lengths
+    (log-uniform in [64, 2^22]) at batches 1 / 64 / 4096 (capped at 2^24
+    elements per launch), a 3-layer MLP (hidden 64, FP32) trained on them on
+    the GPU, then held-out lengths: regret of the model's picks and of the
+    heuristic plan against the exhaustive best, and held-out throughput under
+    each. The library kernels are timed (plan-time compilation off), so the
+    thousands of configurations need no NVRTC compiles."""
+    os.environ["CHFFT_JIT"] = "0"
+    import chfft_gb300 as cg
+    from chfft_gb300 import tuning
+
+    n_train = int(os.environ.get("CHFFT_COSTMODEL_TRAIN", "2000"))
+    n_test = int(os.environ.get("CHFFT_COSTMODEL_TEST", "500"))
+    rng = np.random.default_rng(5)
+    train_len = tuning.log_uniform_lengths(rng, n_train, 64, 1 << 22)
+    test_len = tuning.log_uniform_lengths(rng, n_test, 64, 1 << 22, exclude=train_len)
+    batches = [1, 64, 4096]
+    mk = lambda n: cg.CFft1D.with_len(int(n), np.float32)  # noqa: E731
+    t0 = time.perf_counter()
+    prog = lambda i: (i % 100 == 0) and print(f"  {i} lengths, {time.perf_counter() - t0:.0f} s",  # noqa: E731
+                                              file=sys.stderr, flush=True)
+    tr = tuning.collect(mk, train_len, batches, max_elems=1 << 24, reps=3, progress=prog)
+    te = tuning.collect(mk, test_len, batches, max_elems=1 << 24, reps=3, progress=prog)
+    t_collect = time.perf_counter() - t0
+    X, y = tuning.dataset(tr)
+    model = tuning.CostModel(64, seed=0)
+    t1 = time.perf_counter()
+    loss = model.train(X, y, epochs=200, batch=256, lr=2e-3)
+    t_train = time.perf_counter() - t1
+    pick, heur = tuning.regret(te, model)
+    flops = np.array([5.0 * s.length * math.log2(s.length) * s.batch for s in te])
+    t_best = np.array([float(s.ms.min()) for s in te])
+    t_pick = pick * t_best
+    t_heur = heur * t_best
+    gf = lambda t: round(float(flops.sum() / (t.sum() * 1e-3) / 1e9), 2)  # noqa: E731
+    line = {
+        "metric": METRIC, "value": gf(t_pick), "unit": "GFLOP/s", "n_gpus": 1, "steps": len(te),
+        "warmup": 1, "ms_per_step": round(float(t_pick.sum()) / len(te), 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (device scratch bytes 0x3c); lengths log-uniform in [64, 2^22], seeded",
+        "config": {"workload": f"learned plan cost model: {len(train_len)} training lengths x batch {{1, 64, 4096}} "
+                               f"(<= 2^24 elements), {len(test_len)} held-out lengths; CFft1D f32 forward",
+                   "model": "MLP 40-64-64-1 ReLU FP32, Adam, 200 epochs, trained by the library's CUDA kernels",
+                   "timing": "median of 3 CUDA-event launches after 1 warm-up, per candidate",
+                   "kernels": "library kernels (plan-time compilation off)"},
+        "held_out": {
+            "cases": len(te), "train_cases": len(tr), "train_rows": int(len(y)),
+            "regret_model_geomean": round(float(np.exp(np.mean(np.log(pick)))), 4),
+            "regret_heuristic_geomean": round(float(np.exp(np.mean(np.log(heur)))), 4),
+            "within_10pct_model": round(float(np.mean(pick <= 1.10)), 4),
+            "within_10pct_heuristic": round(float(np.mean(heur <= 1.10)), 4),
+            "gflops_model": gf(t_pick), "gflops_exhaustive": gf(t_best), "gflops_heuristic": gf(t_heur),
+            "train_loss": round(float(loss), 5), "train_seconds": round(t_train, 2),
+            "collect_seconds": round(t_collect, 1),
+        },
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -618,8 +709,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["batch", "large", "uneven"], default="batch",
-                    help="batch: the headline configuration (default); large / uneven: the other configurations")
+    ap.add_argument("--workload", choices=["batch", "large", "uneven", "costmodel"], default="batch",
+                    help="batch: the headline configuration (default); large / uneven / costmodel: the others")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -631,6 +722,8 @@ def main():
         return run_uneven(args)
     if args.workload == "large":
         return run_large(args)
+    if args.workload == "costmodel":
+        return run_costmodel(args)
     if world > 1:
         import torch
 

@@ -21,7 +21,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden", "-I", INCLUDE, "-I", BUILD]
 # Kernel headers the plan-time compiler (csrc/jit.cu) hands to NVRTC.
-JIT_HEADERS = ["common.cuh", "engine.cuh", "kernels.cuh", "k_complex.cuh", "k_real.cuh"]
+JIT_HEADERS = ["common.cuh", "engine.cuh", "kernels.cuh", "k_complex.cuh", "k_real.cuh", "tc.cuh", "tc_core.cuh"]
 
 
 def _gen_jit_headers() -> None:

@@ -156,7 +156,7 @@ bool build_big(HostBig& hb, long long n, bool blue_ok, cudaStream_t s) {
   }
   hb.m = m;
   if (!build_small(hb.ca, n1, s) || !build_small(hb.cb, n2, s) || hb.ca.d.blue || hb.cb.d.blue) return false;
-  const int L = (int)std::ceil(std::sqrt((double)m));
+  const int sh = tw_shift_for(m), L = 1 << sh;
   const long long nhi = (m + L - 1) / L;
   hb.lo.ensure(L * 8);
   hb.hi.ensure(nhi * 8);
@@ -171,7 +171,7 @@ bool build_big(HostBig& hb, long long n, bool blue_ok, cudaStream_t s) {
   hb.fs.n = m;
   hb.fs.n1 = n1;
   hb.fs.n2 = n2;
-  hb.fs.tw_l = L;
+  hb.fs.tw_shift = sh;
   hb.fs.lo = hb.lo.p;
   hb.fs.hi = hb.hi.p;
   hb.fs.n_user = n;

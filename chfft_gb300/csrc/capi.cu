@@ -1,347 +1,12 @@
 // The C ABI (include/chfft_gpu.h): plan objects mirroring chfft's five plan
 // types, their setup methods and the per-method (direction, scale) table.
-#include <cmath>
-#include <cstring>
 #include <functional>
 #include <new>
-#include <string>
-#include <vector>
 
-#include "../../include/chfft_gpu.h"
-#include "jit.hpp"
-#include "plan.hpp"
-
-namespace chfft {
-namespace {
-
-thread_local std::string tl_error;
-
-int set_error(int code, const std::string& msg) {
-  tl_error = msg;
-  return code;
-}
-
-enum ScaleKind { S_ONE, S_UNITARY, S_N, S_DCT_U, S_DCT_N, S_MDCT_UI, S_MDCT_U };
-
-struct MethodSpec {
-  bool ok = false;
-  bool back = false;
-  ScaleKind scale = S_ONE;
-};
-
-// The reference's method table per type: CFft1D (src/cfft1d.rs:270-455),
-// CFft2D (src/cfft2d.rs:150-321), RFft1D (src/rfft1d.rs:199-313),
-// Dct1D (src/dct1d.rs:98-144), Mdct1D (src/mdct1d.rs:149-195).
-MethodSpec method_spec(int kind, int m) {
-  MethodSpec s;
-  auto set = [&](bool back, ScaleKind k) {
-    s.ok = true;
-    s.back = back;
-    s.scale = k;
-  };
-  switch (kind) {
-    case CHFFT_KIND_CFFT1D:
-    case CHFFT_KIND_CFFT2D:
-    case CHFFT_KIND_RFFT1D:
-      switch (m) {
-        case CHFFT_FORWARD: case CHFFT_FORWARD0: set(false, S_ONE); break;
-        case CHFFT_FORWARDU: set(false, S_UNITARY); break;
-        case CHFFT_FORWARDN: set(false, S_N); break;
-        case CHFFT_BACKWARD: set(true, S_N); break;
-        case CHFFT_BACKWARD0: set(true, S_ONE); break;
-        case CHFFT_BACKWARDU: set(true, S_UNITARY); break;
-        case CHFFT_BACKWARDN: if (kind != CHFFT_KIND_CFFT2D) set(true, S_N); break;
-        case CHFFT_FORWARD0I: if (kind == CHFFT_KIND_CFFT1D) set(false, S_ONE); break;
-        case CHFFT_BACKWARD0I: if (kind == CHFFT_KIND_CFFT1D) set(true, S_ONE); break;
-        case CHFFT_FORWARDUI: if (kind == CHFFT_KIND_CFFT1D) set(false, S_UNITARY); break;
-        case CHFFT_BACKWARDUI: if (kind == CHFFT_KIND_CFFT1D) set(true, S_UNITARY); break;
-        default: break;
-      }
-      break;
-    case CHFFT_KIND_DCT1D:
-      switch (m) {
-        case CHFFT_FORWARD: case CHFFT_FORWARD0: set(false, S_ONE); break;
-        case CHFFT_FORWARDU: set(false, S_DCT_U); break;
-        case CHFFT_FORWARDN: set(false, S_DCT_N); break;
-        default: break;
-      }
-      break;
-    case CHFFT_KIND_MDCT1D:
-      switch (m) {
-        case CHFFT_FORWARD: set(false, S_MDCT_UI); break;
-        case CHFFT_FORWARDU: set(false, S_ONE); break;
-        case CHFFT_BACKWARD: set(true, S_MDCT_U); break;
-        case CHFFT_BACKWARDU: set(true, S_ONE); break;
-        default: break;
-      }
-      break;
-    default: break;
-  }
-  return s;
-}
-
-}  // namespace
-
-struct PlanImpl {
-  int kind = 0, dtype = 0;
-  long long len = 0, len_m = 0, len_n = 0;
-  int dct_type = CHFFT_DCT_TWO;
-  bool ortho = false;
-  int window = CHFFT_WINDOW_SINE;
-  std::vector<unsigned char> custom_window;
-  Core core;   // complex core (CFft1D: N; CFft2D rows: N; RFft1D/Dct1D: N/2; Mdct1D: N/4)
-  Core core2;  // CFft2D columns: M
-  BigCore big;           // CFft1D beyond one CTA (four-step)
-  bool use_big = false;
-  DevBuf work;           // four-step workspace
-  DevBuf aux0, aux1;
-  cudaStream_t stream = nullptr;
-  DevBuf stage_in, stage_out;
-
-  ~PlanImpl() {
-    if (stream) cudaStreamDestroy(stream);
-  }
-
-  cudaStream_t host_stream() {
-    if (!stream) CHFFT_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-    return stream;
-  }
-
-  // (Re)build every table for the current lengths. Returns a status.
-  int build() {
-    cudaStream_t s = host_stream();
-    aux0.release();
-    aux1.release();
-    const size_t cb = cplx_bytes(dtype), rb = real_bytes(dtype);
-    auto gen = [&](Table t, long long n, long long count, void* out) {
-      CHFFT_CUDA(dtype == 0 ? gen_table<float>(t, n, count, 0, out, s) : gen_table<double>(t, n, count, 0, out, s));
-    };
-    auto need = [&](Core& c, long long n) {
-      if (!c.build(n, dtype, s)) throw Fail{CHFFT_EUNSUPPORTED, "transform length " + std::to_string(n) + " exceeds the shared-memory engine"};
-    };
-    use_big = false;
-    switch (kind) {
-      case CHFFT_KIND_CFFT1D:
-        if (len >= 2 && !core.build(len, dtype, s)) {
-          if (!big.build(len, dtype, s))
-            throw Fail{CHFFT_EUNSUPPORTED, "transform length " + std::to_string(len) + " is not supported"};
-          use_big = true;
-        }
-        break;
-      case CHFFT_KIND_CFFT2D:
-        if (len_m > 0 && len_n > 0) {
-          need(core, len_n);
-          need(core2, len_m);
-        }
-        break;
-      case CHFFT_KIND_RFFT1D: {
-        long long h = len / 2;
-        need(core, h);
-        aux0.ensure(h * cb);
-        aux1.ensure(h * cb);
-        gen(Table::RCOEF, len, h, aux0.p);
-        gen(Table::RBCOEF, len, h, aux1.p);
-        break;
-      }
-      case CHFFT_KIND_DCT1D: {
-        long long h = len / 2;
-        need(core, h);
-        aux0.ensure(h * cb);
-        aux1.ensure((h + 1) * cb);
-        gen(dct_type == CHFFT_DCT_TWO ? Table::RCOEF : Table::RBCOEF, len, h, aux0.p);
-        gen(dct_type == CHFFT_DCT_TWO ? Table::OMEGA4N_POS : Table::OMEGA4N_NEG, len, h + 1, aux1.p);
-        break;
-      }
-      case CHFFT_KIND_MDCT1D: {
-        long long q = len / 4;
-        need(core, q);
-        aux0.ensure(q * cb);
-        aux1.ensure(len * rb);
-        gen(Table::MDCT_TW, len, q, aux0.p);
-        if (window == CHFFT_WINDOW_CUSTOM)
-          CHFFT_CUDA(cudaMemcpyAsync(aux1.p, custom_window.data(), len * rb, cudaMemcpyHostToDevice, s));
-        else
-          gen(window == CHFFT_WINDOW_VORBIS ? Table::VORBIS_WIN : Table::SINE_WIN, len, len, aux1.p);
-        break;
-      }
-    }
-    CHFFT_CUDA(cudaStreamSynchronize(s));
-    return CHFFT_OK;
-  }
-
-  // Elements (of the side's own type) per transform for a method direction.
-  size_t in_elems(bool back) const {
-    switch (kind) {
-      case CHFFT_KIND_CFFT1D: return (size_t)len;
-      case CHFFT_KIND_CFFT2D: return (size_t)(len_m * len_n);
-      case CHFFT_KIND_RFFT1D: return back ? (size_t)(len / 2 + 1) : (size_t)len;
-      case CHFFT_KIND_DCT1D: return (size_t)len;
-      default: return back ? (size_t)(len / 2) : (size_t)len;
-    }
-  }
-  size_t out_elems(bool back) const {
-    switch (kind) {
-      case CHFFT_KIND_RFFT1D: return back ? (size_t)len : (size_t)(len / 2 + 1);
-      case CHFFT_KIND_MDCT1D: return back ? (size_t)len : (size_t)(len / 2);
-      default: return in_elems(back);
-    }
-  }
-  // Bytes per element of the input / output side.
-  size_t in_esize(bool back) const {
-    switch (kind) {
-      case CHFFT_KIND_CFFT1D: case CHFFT_KIND_CFFT2D: return cplx_bytes(dtype);
-      case CHFFT_KIND_RFFT1D: return back ? cplx_bytes(dtype) : real_bytes(dtype);
-      default: return real_bytes(dtype);
-    }
-  }
-  size_t out_esize(bool back) const {
-    if (kind == CHFFT_KIND_RFFT1D) return back ? real_bytes(dtype) : cplx_bytes(dtype);
-    return in_esize(back);
-  }
-
-  double scale_value(ScaleKind k) const {
-    double n = kind == CHFFT_KIND_CFFT2D ? (double)len_m * (double)len_n : (double)len;
-    switch (k) {
-      case S_ONE: return 1.0;
-      case S_UNITARY: return 1.0 / std::sqrt(n);
-      case S_N: return 1.0 / n;
-      case S_DCT_U: return std::sqrt(2.0 / n);
-      case S_DCT_N: return 2.0 / n;
-      case S_MDCT_UI: return std::sqrt(n / 2.0);
-      case S_MDCT_U: return 1.0 / std::sqrt(n / 2.0);
-    }
-    return 1.0;
-  }
-
-  // Plan-time specialised kernel when the plan compiler is on for this batch
-  // size (CHFFT_JIT: auto = batches of >= 2^18 elements), else the library
-  // kernel with run-time stages.
-  template <typename T>
-  void dispatch(Kernel k, const Core& c, const Geo& g, const KArgs& a, unsigned blocks, long long elems,
-                cudaStream_t s) {
-    const JitMode mode = jit_mode();
-    const bool want = c.st.n > 1 && (mode == JitMode::ALWAYS || (mode == JitMode::AUTO && elems >= (1LL << 18)));
-    if (want) {
-      int r = jit_launch(k, dtype, c, g, a, blocks, s);
-      if (r == 0) return;
-      if (r == 2) throw Fail{CHFFT_ECUDA, "launch of a plan-time specialised kernel failed"};
-    }
-    CHFFT_CUDA(launch_kernel<T>(k, c.blue, g.k1, a, blocks, g.threads, g.smem, s));
-  }
-
-  template <typename T>
-  void launch(Kernel k, const Core& c, KArgs& a, long long count, cudaStream_t s) {
-    Geo g = row_geo(c, count);
-    a.core = c.desc();
-    a.tpb = g.tpb;
-    a.ld = g.ld;
-    a.count = count;
-    unsigned blocks = (unsigned)((count + g.tpb - 1) / g.tpb);
-    dispatch<T>(k, c, g, a, blocks, count * c.n, s);
-  }
-
-  template <typename T>
-  void exec_t(const MethodSpec& ms, const void* d_in, void* d_out, long long batch, cudaStream_t s) {
-    const double sc = scale_value(ms.scale);
-    KArgs a{};
-    a.in = d_in;
-    a.out = d_out;
-    a.scale = sc;
-    a.back = ms.back ? 1 : 0;
-    switch (kind) {
-      case CHFFT_KIND_CFFT1D:
-        if (len <= 1) {  // chfft returns a copy for len <= 1 (src/cfft1d.rs:212-214)
-          if (d_in != d_out && len == 1)
-            CHFFT_CUDA(cudaMemcpyAsync(d_out, d_in, batch * cplx_bytes(dtype), cudaMemcpyDeviceToDevice, s));
-          return;
-        }
-        if (use_big) {
-          work.ensure((size_t)big.work_elems(batch) * cplx_bytes(dtype));
-          big.exec(d_in, d_out, work.p, batch, ms.back, sc, s);
-          return;
-        }
-        a.in_dist = a.out_dist = len;
-        launch<T>(Kernel::C2C, core, a, batch, s);
-        return;
-      case CHFFT_KIND_CFFT2D: {
-        if (len_m == 0 || len_n == 0) return;
-        // Row FFTs of length N into d_out, then column FFTs of length M in
-        // place with the scale (src/cfft2d.rs:340-361).
-        a.in_dist = a.out_dist = len_n;
-        a.scale = 1.0;
-        launch<T>(Kernel::C2C, core, a, batch * len_m, s);
-        KArgs b{};
-        b.core = core2.desc();
-        Geo g = col_geo(core2, (int)len_n);
-        b.tpb = g.tpb;
-        b.ld = g.ld;
-        b.back = a.back;
-        b.count = batch;
-        b.tiles_per_tr = (len_n + g.tpb - 1) / g.tpb;
-        b.in = d_out;
-        b.out = d_out;
-        b.scale = sc;
-        b.in_dist = b.out_dist = len_m * len_n;
-        b.ncols = (int)len_n;
-        dispatch<T>(Kernel::COLS, core2, g, b, (unsigned)(batch * b.tiles_per_tr), batch * len_m * len_n, s);
-        return;
-      }
-      case CHFFT_KIND_RFFT1D:
-        a.aux0 = ms.back ? aux1.p : aux0.p;
-        a.in_dist = ms.back ? len / 2 + 1 : len;
-        a.out_dist = ms.back ? len : len / 2 + 1;
-        launch<T>(ms.back ? Kernel::C2R : Kernel::R2C, core, a, batch, s);
-        return;
-      case CHFFT_KIND_DCT1D:
-        a.aux0 = aux0.p;
-        a.aux1 = aux1.p;
-        a.in_dist = a.out_dist = len;
-        // ortho: x0 * sqrt(1/2) (DCT-II) or 1/2 -> sqrt(1/2) (DCT-III) (src/dct1d.rs:220-224, :343-347)
-        a.aux_scalar = ortho ? std::sqrt(0.5) : (dct_type == CHFFT_DCT_TWO ? 1.0 : 0.5);
-        launch<T>(dct_type == CHFFT_DCT_TWO ? Kernel::DCT2 : Kernel::DCT3, core, a, batch, s);
-        return;
-      case CHFFT_KIND_MDCT1D:
-        a.aux0 = aux0.p;
-        a.aux1 = aux1.p;
-        a.n_user = (int)len;
-        a.in_dist = ms.back ? len / 2 : len;
-        a.out_dist = ms.back ? len : len / 2;
-        launch<T>(ms.back ? Kernel::IMDCT : Kernel::MDCT, core, a, batch, s);
-        return;
-    }
-  }
-
-  void exec(const MethodSpec& ms, const void* d_in, void* d_out, long long batch, cudaStream_t s) {
-    if (batch <= 0) return;
-    if (dtype == CHFFT_F32)
-      exec_t<float>(ms, d_in, d_out, batch, s);
-    else
-      exec_t<double>(ms, d_in, d_out, batch, s);
-  }
-
-  // Host memory: stage in, run, stage out, synchronise.
-  void exec_host(const MethodSpec& ms, const void* src, void* dst, long long batch) {
-    cudaStream_t s = host_stream();
-    const size_t ib = in_elems(ms.back) * in_esize(ms.back) * batch;
-    const size_t ob = out_elems(ms.back) * out_esize(ms.back) * batch;
-    if (ib == 0 && ob == 0) return;
-    stage_in.ensure(ib);
-    stage_out.ensure(ob);
-    if (ib) CHFFT_CUDA(cudaMemcpyAsync(stage_in.p, src, ib, cudaMemcpyHostToDevice, s));
-    exec(ms, stage_in.p, stage_out.p, batch, s);
-    if (ob) CHFFT_CUDA(cudaMemcpyAsync(dst, stage_out.p, ob, cudaMemcpyDeviceToHost, s));
-    CHFFT_CUDA(cudaStreamSynchronize(s));
-  }
-};
-
-}  // namespace chfft
+#include "plan_impl.hpp"
 
 using chfft::Fail;
 using chfft::PlanImpl;
-
-struct chfft_plan_s {
-  PlanImpl impl;
-};
 
 namespace {
 

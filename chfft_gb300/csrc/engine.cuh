@@ -27,10 +27,13 @@
 namespace chfft {
 
 constexpr int kMaxThreads = 512;  // threads per CTA, every kernel
-constexpr int kNumRadix = 8;
-// Canonical radix order of the shared-memory passes.
+constexpr int kTcThreads = 256;   // threads per CTA of the tensor-core core (tc_core.cuh)
+constexpr int kNumRadix = 9;
+// Canonical radix order of the shared-memory passes. Radix 32 (last) only
+// appears in the stage lists of compile-time-stage kernels with 32 elements
+// per thread (f32): the run-time-stage loops below cover the first eight.
 CHFFT_HD constexpr int radix_at(int i) {
-  return i == 0 ? 16 : i == 1 ? 8 : i == 2 ? 4 : i == 3 ? 2 : i == 4 ? 10 : i == 5 ? 5 : i == 6 ? 3 : 7;
+  return i == 0 ? 16 : i == 1 ? 8 : i == 2 ? 4 : i == 3 ? 2 : i == 4 ? 10 : i == 5 ? 5 : i == 6 ? 3 : i == 7 ? 7 : 32;
 }
 
 // Complex elements one thread holds during a pass: 32 (64 registers) for
@@ -99,6 +102,7 @@ template <int R, bool TMINOR, bool K1, bool STW = false, int EPT = 0, typename C
 __device__ __forceinline__ void pass_body(int n, int Ns, int tpb, const C* __restrict__ tw, const Ld& ld,
                                           const St& st) {
   constexpr int K = K1 ? 1 : (EPT > 0 ? EPT : Ept<C>::value) / R;
+  static_assert(K >= 1, "radix larger than the per-thread element budget");
   const int nb = n / R;
   const int total = tpb * nb;
   const int tw_step = (Ns > 1) ? n / (Ns * R) : 0;
@@ -234,6 +238,7 @@ struct CoreDesc {
   const void* chirp;  // Bluestein: c_j, j < n
   const void* bhat;   // Bluestein: FFT_M(conj c) / M
   const void* stw;    // stage twiddles of the fused pass order (compile-time-stage kernels)
+  int* err;           // device error word (tensor-core cores: 2 = an MMA wait timed out), may be null
 };
 
 // Y <- conj(Y * B^) on every sequence of the tile.
@@ -309,6 +314,7 @@ __device__ __forceinline__ void core_fft(const CoreDesc& d, int tpb, const SmemI
 template <bool BLUE, bool TMINOR, bool FUSED, bool K1>
 struct DynCore {
   static constexpr bool kK1 = K1;
+  static constexpr bool kStatic = false;
   // The kernel's shared-memory tile (layout shared with the kernel's own
   // pre-/post-phases).
   template <typename C>
@@ -324,16 +330,20 @@ struct DynCore {
 
 // Passes R, Rest... with Ns = NS at the first and this pass's stage-table
 // block at stw + OFF: `ld` feeds the first pass, `st` takes the last, the
-// tile carries everything in between.
-template <int N, int TPB, int LD, int P, bool TMINOR, bool K1, int NS, int OFF, int R, int... Rest, typename C,
-          class Ld, class St>
+// tile carries everything in between. ROWS_FIRST maps the first pass's
+// threads along each sequence (coalesced loads of contiguous rows) whatever
+// TMINOR says for the others; any mapping of a pass's butterflies to threads
+// computes the same transform.
+template <int N, int TPB, int LD, int P, bool TMINOR, bool K1, int NS, int OFF, bool ROWS_FIRST, int R, int... Rest,
+          typename C, class Ld, class St>
 __device__ __forceinline__ void static_passes(const C* stw, C* s, const Ld& ld, const St& st) {
+  constexpr bool kMinor = TMINOR && !(ROWS_FIRST && OFF == 0);
   if constexpr (sizeof...(Rest) == 0) {
-    pass_body<R, TMINOR, K1, true>(N, NS, TPB, stw + OFF, ld, st);
+    pass_body<R, kMinor, K1, true>(N, NS, TPB, stw + OFF, ld, st);
   } else {
     const SmemIO<C, P> sm{s, LD};
-    pass_body<R, TMINOR, K1, true>(N, NS, TPB, stw + OFF, ld, sm);
-    static_passes<N, TPB, LD, P, TMINOR, K1, NS * R, OFF + (R - 1) * NS, Rest...>(stw, s, sm, st);
+    pass_body<R, kMinor, K1, true>(N, NS, TPB, stw + OFF, ld, sm);
+    static_passes<N, TPB, LD, P, TMINOR, K1, NS * R, OFF + (R - 1) * NS, ROWS_FIRST, Rest...>(stw, s, sm, st);
   }
 }
 
@@ -351,23 +361,26 @@ struct SpectrumStore {
 template <bool BLUE, bool TMINOR, bool K1, int M, int NU, int TPB, int LD, int P, int... Rs>
 struct StatCore {
   static constexpr bool kK1 = K1;
+  static constexpr bool kStatic = true;
   template <typename C>
   __device__ __forceinline__ static SmemIO<C, P> tile(unsigned char* base, int) {
     return SmemIO<C, P>{reinterpret_cast<C*>(base), LD};
   }
-  template <typename C, class Ld, class St>
+  // ROWS_FIRST: `ld` reads contiguous sequences, so the first pass maps
+  // threads along them (the column-mapped transposing row pass).
+  template <bool ROWS_FIRST = false, typename C, class Ld, class St>
   __device__ __forceinline__ static void run(const CoreDesc& d, int, const SmemIO<C, P>& sm, const Ld& ld,
                                              const St& st) {
     const C* stw = static_cast<const C*>(d.stw);
     if constexpr (!BLUE) {
-      static_passes<M, TPB, LD, P, TMINOR, K1, 1, 0, Rs...>(stw, sm.s, ld, st);
+      static_passes<M, TPB, LD, P, TMINOR, K1, 1, 0, ROWS_FIRST, Rs...>(stw, sm.s, ld, st);
     } else {
       const C* chirp = static_cast<const C*>(d.chirp);
       ChirpIn<C, Ld> l1{ld, chirp, NU};
       ChirpOut<C, St> s2{st, chirp, NU};
       SpectrumStore<C, SmemIO<C, P>> spec{sm, static_cast<const C*>(d.bhat)};
-      static_passes<M, TPB, LD, P, TMINOR, K1, 1, 0, Rs...>(stw, sm.s, l1, spec);
-      static_passes<M, TPB, LD, P, TMINOR, K1, 1, 0, Rs...>(stw, sm.s, sm, s2);
+      static_passes<M, TPB, LD, P, TMINOR, K1, 1, 0, ROWS_FIRST, Rs...>(stw, sm.s, l1, spec);
+      static_passes<M, TPB, LD, P, TMINOR, K1, 1, 0, false, Rs...>(stw, sm.s, sm, s2);
     }
   }
 };

@@ -11,6 +11,7 @@
 // run-time-stage kernels compiled into the library.
 #include <dlfcn.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -133,7 +134,20 @@ int pad_period(const StageList& st) {
 bool column_mapped(Kernel k) { return k == Kernel::COLS || k == Kernel::COLS_TW || k == Kernel::ROWS_T; }
 bool four_step(Kernel k) { return k == Kernel::COLS_TW || k == Kernel::ROWS_T; }
 
-std::string name_expression(Kernel k, int dtype, const Core& c, const Geo& g, int mode) {
+// Tile stride of a specialised kernel. Column-mapped passes give the lanes
+// of one shared-memory wavefront (16 f32 / 8 f64 complex elements) tpb
+// adjacent sequences times q = lanes / tpb adjacent elements; a stride that
+// is q times an odd number puts all of them in distinct banks.
+int tile_ld(const StageList& st, int tpb, int dtype, bool column) {
+  const int p = pad_period(st);
+  int ld = st.n + (p > 0 ? st.n / p : 0);
+  const int lanes = dtype == 0 ? 16 : 8;
+  const int q = column ? std::max(1, lanes / std::max(1, tpb)) : 1;
+  while (ld % (2 * q) != q) ld++;
+  return ld;
+}
+
+std::string name_expression(Kernel k, int dtype, const Core& c, const StageList& sl, const Geo& g, int mode) {
   std::string s = "&";
   s += kernel_template(k);
   s += dtype == 0 ? "<float, " : "<double, ";
@@ -141,9 +155,9 @@ std::string name_expression(Kernel k, int dtype, const Core& c, const Geo& g, in
   s += c.blue ? "true," : "false,";
   s += column_mapped(k) ? "true," : "false,";
   s += g.k1 ? "true," : "false,";
-  s += std::to_string(c.st.n) + "," + std::to_string(c.n) + "," + std::to_string(g.tpb) + "," + std::to_string(g.ld) +
-       "," + std::to_string(pad_period(c.st));
-  for (int r : pass_order(c.st)) s += "," + std::to_string(r);
+  s += std::to_string(sl.n) + "," + std::to_string(c.n) + "," + std::to_string(g.tpb) + "," + std::to_string(g.ld) +
+       "," + std::to_string(pad_period(sl));
+  for (int r : pass_order(sl)) s += "," + std::to_string(r);
   s += ">";
   if (four_step(k)) s += ", " + std::to_string(mode);
   s += ">";
@@ -152,7 +166,7 @@ std::string name_expression(Kernel k, int dtype, const Core& c, const Geo& g, in
 
 bool compile(const std::string& expr, Entry* e, std::string* log) {
   nvrtcProgram prog = nullptr;
-  const char* src = "#include \"k_complex.cuh\"\n#include \"k_real.cuh\"\n";
+  const char* src = "#include \"k_complex.cuh\"\n#include \"k_real.cuh\"\n#include \"tc_core.cuh\"\n";
   if (g_api.nvrtcCreateProgram(&prog, src, "chfft_plan.cu", kJitHeaderCount, kJitHeaderSrc, kJitHeaderNames) != 0) {
     *log = "nvrtcCreateProgram failed";
     return false;
@@ -207,16 +221,29 @@ int jit_launch(Kernel k, int dtype, const Core& c, const Geo& g0, const KArgs& a
   std::lock_guard<std::mutex> lk(g_mu);
   if (!load_api()) return 1;
   if (!c.stw.p) return 1;
+  // Stage list: the radix-32 one where every thread holds 32 elements.
+  const bool wide = !g0.k1 && g0.max_radix >= 32 && c.wide.p;
+  const StageList& sl = wide ? c.sw : c.st;
   // The specialised tile uses its own pad period, hence its own stride.
   Geo g = g0;
-  g.ld = smem_ld(c.st.n, pad_period(c.st));
+  g.ld = tile_ld(sl, g.tpb, dtype, column_mapped(k));
   g.smem = (size_t)g.tpb * g.ld * cplx_bytes(dtype);
   if (g.smem > kMaxSmem) return 1;
+  if (wide) {
+    int th = threads_needed(sl, ept_of(dtype), g.tpb, false);
+    th = std::max(32, ((th + 31) / 32) * 32);
+    if (th > kMaxThreads) return 1;
+    g.threads = th;
+  }
   KArgs a = a0;
   a.ld = g.ld;
+  if (wide) {
+    a.core.st = sl;
+    a.core.stw = c.wide.p;
+  }
   int dev = 0;
   cudaGetDevice(&dev);
-  const std::string expr = name_expression(k, dtype, c, g, mode);
+  const std::string expr = name_expression(k, dtype, c, sl, g, mode);
   Entry& e = g_cache[std::to_string(dev) + "|" + expr];
   if (e.failed) return 1;
   if (!e.fn) {
@@ -233,6 +260,67 @@ int jit_launch(Kernel k, int dtype, const Core& c, const Geo& g0, const KArgs& a
   }
   void* args[] = {const_cast<KArgs*>(&a), const_cast<FourStep*>(fs)};
   if (g_api.cuLaunchKernel(e.fn, blocks, 1, 1, g.threads, 1, 1, (unsigned)g.smem, (CUstream)stream, args, nullptr) != 0)
+    return 2;
+  return 0;
+}
+
+size_t tc_geometry(const Core& c, Kernel k, int tpb, int prec, int* ld_out) {
+  if (c.dtype != 0 || c.blue || c.tc_s16 < 1 || !c.tcw.p || prec < 1 || prec > 3 || tpb < 1) return 0;
+  const long long n = c.st.n;
+  const long long rows = (long long)tpb * (n / 16);
+  if (rows % 128 || rows / 128 > 16) return 0;
+  int ld = (int)(n + n / 16);
+  const int q = column_mapped(k) ? std::max(1, 16 / tpb) : 1;
+  while (ld % (2 * q) != q) ld++;
+  const size_t tile = (size_t)tpb * ld * 8;
+  const size_t a_off = (tile + 1023) / 1024 * 1024;
+  const size_t np = prec == 3 ? 3 : 2;
+  const size_t smem = a_off + (size_t)(rows / 128) * np * 8192 + np * 2048 + 16;
+  if (smem > kMaxSmem) return 0;
+  if (ld_out) *ld_out = ld;
+  return smem;
+}
+
+int jit_launch_tc(Kernel k, const Core& c, int prec, int tpb, const KArgs& a0, unsigned blocks, cudaStream_t stream,
+                  int mode, const FourStep* fs) {
+  if (four_step(k) && !fs) return 1;
+  if (k != Kernel::C2C && !four_step(k)) return 1;
+  int ld = 0;
+  const size_t smem = tc_geometry(c, k, tpb, prec, &ld);
+  if (!smem) return 1;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!load_api()) return 1;
+  std::string expr = "&";
+  expr += kernel_template(k);
+  expr += "<float, chfft::TcCore<";
+  expr += column_mapped(k) ? "true," : "false,";
+  expr += std::to_string(c.st.n) + "," + std::to_string(tpb) + "," + std::to_string(ld) + "," + std::to_string(prec) +
+          "," + std::to_string(c.tc_r0) + "," + std::to_string(c.tc_s16) + ">";
+  if (four_step(k)) expr += ", " + std::to_string(mode);
+  expr += ">";
+  KArgs a = a0;
+  a.ld = ld;
+  a.tpb = tpb;
+  a.core.stw = c.tcw.p;
+  a.core.err = a0.err;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  Entry& e = g_cache[std::to_string(dev) + "|" + expr];
+  if (e.failed) return 1;
+  if (!e.fn) {
+    std::string log;
+    if (!compile(expr, &e, &log)) {
+      e.failed = true;
+      if (std::getenv("CHFFT_JIT_VERBOSE")) fprintf(stderr, "chfft plan-time compile failed for %s:\n%s\n", expr.c_str(), log.c_str());
+      return 1;
+    }
+  }
+  if ((int)smem > 48 * 1024 && e.smem_set < (int)smem) {
+    if (g_api.cuFuncSetAttribute(e.fn, kAttrMaxDynSmem, (int)smem) != 0) return 2;
+    e.smem_set = (int)smem;
+  }
+  void* args[] = {const_cast<KArgs*>(&a), const_cast<FourStep*>(fs)};
+  if (g_api.cuLaunchKernel(e.fn, blocks, 1, 1, kTcThreads, 1, 1, (unsigned)smem, (CUstream)stream, args, nullptr) != 0)
     return 2;
   return 0;
 }

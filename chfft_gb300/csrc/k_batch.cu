@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_batch(const BatchArgs A) {
         const int col = c0 + t;
         if (col >= fs.n2) continue;
         const long long e = (long long)k1 * col;
-        const C tw = cmul(__ldg(&hi[e / fs.tw_l]), __ldg(&lo[e % fs.tw_l]));
+        const C tw = cmul(__ldg(&hi[e >> fs.tw_shift]), __ldg(&lo[e & ((1LL << fs.tw_shift) - 1)]));
         w[(long long)k1 * fs.n2 + col] = cmul(sm.load(t, k1), tw);
       }
     } else {  // BT_FS_B: X[k1 + n1 k2]

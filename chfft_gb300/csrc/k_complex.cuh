@@ -97,7 +97,8 @@ __global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_cols(const 
 // A length-N FFT with N = N1 * N2 beyond one CTA (x[n1 N2 + n2]):
 //   pass A: column FFTs of length N1, times w_N^(k1 n2), in place layout;
 //   pass B: row FFTs of length N2, written transposed to X[k1 + N1 k2].
-// The inter-pass twiddle comes from two tables: w_N^e = hi[e / L] lo[e % L]
+// The inter-pass twiddle comes from two tables: w_N^e = hi[e / L] lo[e % L],
+// L a power of two so the split is a shift and a mask
 // (FourStep in kernels.cuh).
 
 // Pass A loader: MODE 0 plain (scale, conjugate for backward); MODE 1 the
@@ -133,7 +134,7 @@ struct ColsAStore {
     const long long e = (long long)k1 * (c0 + t);  // < N
     const C* lo = static_cast<const C*>(fs->lo);
     const C* hi = static_cast<const C*>(fs->hi);
-    const C w = cmul(__ldg(&hi[e / fs->tw_l]), __ldg(&lo[e % fs->tw_l]));
+    const C w = cmul(__ldg(&hi[e >> fs->tw_shift]), __ldg(&lo[e & ((1LL << fs->tw_shift) - 1)]));
     out[(long long)k1 * ncols + t] = cmul(v, w);
   }
 };
@@ -196,11 +197,16 @@ __global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_rows_t(cons
   const int nvalid = min(a.tpb, fs.n1 - r0);
   // Rows are contiguous: load them with consecutive threads along a row,
   // then run the FFT with consecutive threads across rows so the transposed
-  // store is contiguous.
+  // store is contiguous. Compile-time-stage cores fuse the row load into
+  // their first pass; the others stage it through the tile.
   RowsBLoad<C> rl{(const C*)a.in + tr * a.in_dist + (long long)r0 * fs.n2, fs.n2, nvalid};
-  load_phase<false>(sm, fs.n2, a.tpb, rl);
   RowsBStore<C, MODE> st{(C*)a.out + tr * a.out_dist, r0, nvalid, fs.n1, a.back, &fs};
-  CoreT::run(a.core, a.tpb, sm, sm, st);
+  if constexpr (CoreT::kStatic) {
+    CoreT::template run<true>(a.core, a.tpb, sm, rl, st);
+  } else {
+    load_phase<false>(sm, fs.n2, a.tpb, rl);
+    CoreT::run(a.core, a.tpb, sm, sm, st);
+  }
 }
 
 }  // namespace kern

@@ -49,7 +49,7 @@ enum class Kernel : int {
 struct FourStep {
   long long n;        // N
   int n1, n2;         // rows (column-FFT length) x row length
-  int tw_l;           // L of the two-level inter-pass twiddle table
+  int tw_shift;       // L = 2^tw_shift, L^2 >= N: the two-level inter-pass twiddle table
   const void* lo;     // w_N^e, e < L
   const void* hi;     // w_N^(e L), e < ceil(N / L)
   long long n_user;   // Bluestein: user length (inputs past it are zero, outputs dropped)

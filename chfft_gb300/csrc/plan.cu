@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdlib>
 
+#include "../../include/chfft_gpu.h"
 #include "jit.hpp"
 
 namespace chfft {
@@ -54,16 +55,17 @@ static int radix_index(int r) {
   return -1;
 }
 
-bool make_stages(long long n, StageList* out) {
+bool make_stages(long long n, StageList* out, int max_radix) {
   StageList st{};
   st.n = (int)n;
   Smooth s = factor_smooth(n);
   if (!s.ok || n > INT_MAX) return false;
+  const int maxbits = max_radix >= 32 ? 5 : 4;
   // t radix-10 passes absorb t twos and t fives; choose t for fewest passes.
   int best_t = 0, best_passes = INT_MAX;
   for (int t = 0; t <= std::min(s.e2, s.e5); t++) {
     int twos = s.e2 - t;
-    int passes = s.e7 + s.e3 + (s.e5 - t) + t + (twos + 3) / 4;
+    int passes = s.e7 + s.e3 + (s.e5 - t) + t + (twos + maxbits - 1) / maxbits;
     if (passes < best_passes || (passes == best_passes && t > best_t)) {
       best_passes = passes;
       best_t = t;
@@ -74,9 +76,9 @@ bool make_stages(long long n, StageList* out) {
   cnt[radix_index(5)] = s.e5 - best_t;
   cnt[radix_index(3)] = s.e3;
   cnt[radix_index(7)] = s.e7;
-  // Powers of two: p = ceil(twos/4) passes of near-equal size.
+  // Powers of two: p = ceil(twos/maxbits) passes of near-equal size.
   int twos = s.e2 - best_t;
-  int p2 = (twos + 3) / 4;
+  int p2 = (twos + maxbits - 1) / maxbits;
   for (int i = 0; i < p2; i++) {
     int bits = twos / p2 + (i < twos % p2 ? 1 : 0);
     cnt[radix_index(1 << bits)]++;
@@ -166,7 +168,35 @@ long long bluestein_length(long long n, int dtype) {
 
 static void fft_f64_inplace(double2* d_data, const Core& c64, cudaStream_t s);
 
-bool Core::build(long long n_, int dtype_, cudaStream_t s) {
+void Core::build_tc(cudaStream_t s) {
+  tc_r0 = tc_s16 = 0;
+  tcw.release();
+  const int m = st.n;
+  if (dtype != 0 || m < 16 || (m & (m - 1))) return;
+  int k = 0;
+  while ((1 << k) < m) k++;
+  PassList pl{};
+  const int r0 = 1 << (k % 4);
+  if (r0 > 1) pl.r[pl.npass++] = r0;
+  for (int i = 0; i < k / 4; i++) pl.r[pl.npass++] = 16;
+  tcw.ensure((size_t)std::max(m - 1, 1) * cplx_bytes(dtype));
+  CHFFT_CUDA(gen_stage_table<float>(pl, tcw.p, s));
+  tc_r0 = r0;
+  tc_s16 = k / 4;
+}
+
+void Core::build_wide(cudaStream_t s) {
+  build_tc(s);
+  sw = st;
+  wide.release();
+  if (dtype != 0 || st.n < 2) return;
+  StageList w;
+  if (!make_stages(st.n, &w, 32) || pass_order(w) == pass_order(st)) return;
+  sw = w;
+  build_stage_table(wide, sw, dtype, s);
+}
+
+bool Core::build(long long n_, int dtype_, cudaStream_t s, long long blue_m) {
   n = n_;
   dtype = dtype_;
   blue = false;
@@ -174,10 +204,14 @@ bool Core::build(long long n_, int dtype_, cudaStream_t s) {
   chirp.release();
   bhat.release();
   stw.release();
+  wide.release();
+  tcw.release();
+  tc_r0 = tc_s16 = 0;
   const size_t cb = cplx_bytes(dtype);
   if (n == 1) {
     st = StageList{};
     st.n = 1;
+    sw = st;
     return true;
   }
   if (make_stages(n, &st) && fits_cta(st, dtype)) {
@@ -185,12 +219,15 @@ bool Core::build(long long n_, int dtype_, cudaStream_t s) {
     CHFFT_CUDA(dtype == 0 ? gen_table<float>(Table::OMEGA, n, n, 0, tw.p, s)
                           : gen_table<double>(Table::OMEGA, n, n, 0, tw.p, s));
     build_stage_table(stw, st, dtype, s);
+    build_wide(s);
     return true;
   }
   // Bluestein core (src/chirpz.rs): chirp table and the spectrum of the
   // conjugate chirp, both from FP64.
   long long m = bluestein_length(n, dtype);
   if (m < 0) return false;
+  StageList sb;
+  if (blue_m >= 2 * n - 1 && make_stages(blue_m, &sb) && fits_cta(sb, dtype)) m = blue_m;
   blue = true;
   make_stages(m, &st);
   tw.ensure(m * cb);
@@ -201,6 +238,7 @@ bool Core::build(long long n_, int dtype_, cudaStream_t s) {
   CHFFT_CUDA(dtype == 0 ? gen_table<float>(Table::CHIRP, n, n, 0, chirp.p, s)
                         : gen_table<double>(Table::CHIRP, n, n, 0, chirp.p, s));
   build_stage_table(stw, st, dtype, s);
+  build_wide(s);
   // B^ = FFT_M(b) / M in FP64 when the f64 engine can run length M in one
   // CTA; otherwise the FFT of the FP64 sequence runs in the working dtype.
   DevBuf b64;
@@ -260,25 +298,27 @@ static void fft_f64_inplace(double2* d_data, const Core& c64, cudaStream_t s) {
   CHFFT_CUDA(launch_kernel<double>(Kernel::C2C, false, g.k1, a, 1, g.threads, g.smem, s));
 }
 
-Geo row_geo(const Core& c, long long count, int target_threads) {
+Geo row_geo(const Core& c, long long count, const PlanOpts& o) {
   Geo g;
+  g.max_radix = o.max_radix == 16 ? 16 : 32;
   const int ept = ept_of(c.dtype);
   const int m = c.st.n;
   g.ld = smem_ld(m);
   const size_t per = (size_t)g.ld * cplx_bytes(c.dtype);
   const int t1k = std::max(1, threads_needed(c.st, ept, 1, true));
-  if (t1k <= kMaxThreads) {
+  const bool k1 = t1k <= kMaxThreads && o.k1 != 0;
+  if (k1) {
     // One butterfly per thread: fill the CTA up to 512 threads, keeping two
     // CTAs' tiles within an SM's shared memory.
     g.k1 = true;
-    int tpb = std::max(1, kMaxThreads / t1k);
-    tpb = (int)std::min<size_t>(tpb, std::max<size_t>(1, (kMaxSmem / 2) / per));
+    int tpb = o.tpb > 0 ? std::min(o.tpb, kMaxThreads / t1k) : std::max(1, kMaxThreads / t1k);
+    tpb = (int)std::min<size_t>(tpb, std::max<size_t>(1, (o.tpb > 0 ? kMaxSmem : kMaxSmem / 2) / per));
     tpb = (int)std::max<long long>(1, std::min<long long>(tpb, count));
     g.tpb = tpb;
   } else {
     const int t1 = std::max(1, threads_needed(c.st, ept, 1));
-    int tpb = std::max(1, target_threads / t1);
-    tpb = (int)std::min<size_t>(tpb, std::max<size_t>(1, (64 * 1024) / per));
+    int tpb = o.tpb > 0 ? o.tpb : std::max(1, 256 / t1);
+    tpb = (int)std::min<size_t>(tpb, std::max<size_t>(1, (o.tpb > 0 ? kMaxSmem : 64 * 1024) / per));
     tpb = (int)std::max<long long>(1, std::min<long long>(tpb, count));
     while (tpb > 1 && threads_needed(c.st, ept, tpb) > kMaxThreads) tpb--;
     g.tpb = tpb;
@@ -290,16 +330,17 @@ Geo row_geo(const Core& c, long long count, int target_threads) {
   return g;
 }
 
-Geo col_geo(const Core& c, int ncols) {
+Geo col_geo(const Core& c, int ncols, int tpb_opt, const PlanOpts& o) {
   Geo g;
+  g.max_radix = o.max_radix == 16 ? 16 : 32;
   const int ept = ept_of(c.dtype);
   g.ld = smem_ld(c.st.n);
   const size_t per = (size_t)g.ld * cplx_bytes(c.dtype);
-  int tpb = c.dtype == 0 ? 16 : 8;  // 128-byte row segments
+  int tpb = tpb_opt > 0 ? tpb_opt : (c.dtype == 0 ? 16 : 8);  // 128-byte row segments
   tpb = std::min(tpb, std::max(1, ncols));
   while (tpb > 1 && ((size_t)tpb * per > kMaxSmem || threads_needed(c.st, ept, tpb) > kMaxThreads)) tpb--;
   g.tpb = tpb;
-  g.k1 = threads_needed(c.st, ept, tpb, true) <= kMaxThreads;
+  g.k1 = o.k1 != 0 && threads_needed(c.st, ept, tpb, true) <= kMaxThreads;
   int th = threads_needed(c.st, ept, tpb, g.k1);
   th = std::max(32, ((th + 31) / 32) * 32);
   g.threads = std::min(th, kMaxThreads);
@@ -307,7 +348,8 @@ Geo col_geo(const Core& c, int ncols) {
   return g;
 }
 
-bool want_specialised(long long elems) {
+bool want_specialised(long long elems, int jit_opt) {
+  if (jit_opt >= 0) return jit_opt == 1;
   const JitMode mode = jit_mode();
   return mode == JitMode::ALWAYS || (mode == JitMode::AUTO && elems >= (1LL << 18));
 }
@@ -334,21 +376,40 @@ bool four_step_split(long long m, int dtype, int* n1, int* n2) {
 }
 
 static void launch_pass(bool pass_a, int mode, const Core& c, const Geo& g, const KArgs& a, const FourStep& fs,
-                        unsigned blocks, long long elems, cudaStream_t s, bool library_only = false) {
-  if (!library_only && want_specialised(elems) &&
+                        unsigned blocks, long long elems, cudaStream_t s, bool library_only, int jit_opt, int tc) {
+  if (tc > 0 && !library_only) {
+    const int r = jit_launch_tc(pass_a ? Kernel::COLS_TW : Kernel::ROWS_T, c, tc, g.tpb, a, blocks, s, mode, &fs);
+    if (r == 2) throw Fail{CHFFT_ECUDA, "launch of a tensor-core kernel failed"};
+    if (r == 1) throw Fail{CHFFT_EUNSUPPORTED, "tensor-core kernel unavailable (plan compiler or geometry)"};
+    return;
+  }
+  if (!library_only && want_specialised(elems, jit_opt) &&
       jit_launch(pass_a ? Kernel::COLS_TW : Kernel::ROWS_T, c.dtype, c, g, a, blocks, s, mode, &fs) == 0)
     return;
   CHFFT_CUDA(c.dtype == 0 ? launch_fourstep<float>(pass_a, mode, g.k1, a, fs, blocks, g.threads, g.smem, s)
                           : launch_fourstep<double>(pass_a, mode, g.k1, a, fs, blocks, g.threads, g.smem, s));
 }
 
-bool BigCore::build(long long n_, int dtype_, cudaStream_t s) {
+bool BigCore::build(long long n_, int dtype_, cudaStream_t s, const PlanOpts& o) {
   n = n_;
   dtype = dtype_;
   blue = false;
   m = n;
+  opts = o;
   const size_t cb_ = cplx_bytes(dtype);
-  if (!four_step_split(n, dtype, &n1, &n2)) {
+  auto split = [&](long long len, int* a1, int* a2) {
+    if (o.fs_n1 > 1 && len % o.fs_n1 == 0) {
+      StageList s1, s2;
+      const long long e = len / o.fs_n1;
+      if (make_stages(o.fs_n1, &s1) && make_stages(e, &s2) && fits_cta(s1, dtype) && fits_cta(s2, dtype)) {
+        *a1 = o.fs_n1;
+        *a2 = (int)e;
+        return true;
+      }
+    }
+    return four_step_split(len, dtype, a1, a2);
+  };
+  if (!split(n, &n1, &n2)) {
     // Bluestein with a four-step M >= 2n - 1 (cheapest by M * passes).
     long long lo_m = 2 * n - 1, hi_m = 1, best_m = -1;
     while (hi_m < lo_m) hi_m <<= 1;
@@ -366,12 +427,14 @@ bool BigCore::build(long long n_, int dtype_, cudaStream_t s) {
       }
     }
     if (best_m < 0) return false;
+    if (o.blue_m >= lo_m && factor_smooth(o.blue_m).ok && four_step_split(o.blue_m, dtype, &n1, &n2)) best_m = o.blue_m;
     blue = true;
     m = best_m;
-    four_step_split(m, dtype, &n1, &n2);
+    split(m, &n1, &n2);
   }
   if (!ca.build(n1, dtype, s) || !cb.build(n2, dtype, s)) return false;
-  tw_l = (int)std::ceil(std::sqrt((double)m));
+  tw_shift = tw_shift_for(m);
+  tw_l = 1 << tw_shift;
   const long long nhi = (m + tw_l - 1) / tw_l;
   lo.ensure(tw_l * cb_);
   hi.ensure(nhi * cb_);
@@ -406,7 +469,7 @@ FourStep BigCore::fs() const {
   f.n = m;
   f.n1 = n1;
   f.n2 = n2;
-  f.tw_l = tw_l;
+  f.tw_shift = tw_shift;
   f.lo = lo.p;
   f.hi = hi.p;
   f.n_user = n;
@@ -416,7 +479,7 @@ FourStep BigCore::fs() const {
 }
 
 long long BigCore::chunk(long long batch) const {
-  long long budget_mb = 64;
+  long long budget_mb = opts.l2_mb > 0 ? opts.l2_mb : 64;
   if (const char* e = std::getenv("CHFFT_L2_BUDGET_MB")) budget_mb = std::max(1LL, std::atoll(e));
   const long long per = m * (long long)cplx_bytes(dtype) * (blue ? 2 : 1);
   return std::max(1LL, std::min(batch, (budget_mb << 20) / per));
@@ -431,7 +494,20 @@ void BigCore::exec(const void* in, void* out, void* work, long long batch, bool 
   char* tmp = static_cast<char*>(work);
   char* tmp2 = tmp + g * m * cb_;
   const FourStep f = fs();
-  const Geo ga = col_geo(ca, n2), gb = col_geo(cb, n1);
+  Geo ga = col_geo(ca, n2, opts.fs_tpb, opts), gb = col_geo(cb, n1, opts.fs_tpb, opts);
+  const int tc = library_only ? 0 : opts.tc;
+  if (tc > 0) {
+    // Tile widths the tensor-core kernels take (largest first, from the knob).
+    auto tile = [&](const Core& c, Kernel k) {
+      for (int t = opts.fs_tpb > 0 ? opts.fs_tpb : 16; t >= 1; t /= 2)
+        if (tc_geometry(c, k, t, tc, nullptr)) return t;
+      return 0;
+    };
+    ga.tpb = tile(ca, Kernel::COLS_TW);
+    gb.tpb = tile(cb, Kernel::ROWS_T);
+    if (!ga.tpb || !gb.tpb)
+      throw Fail{CHFFT_EUNSUPPORTED, "tensor-core passes need power-of-two four-step factors >= 16"};
+  }
   for (long long c0 = 0; c0 < batch; c0 += g) {
     const long long cnt = std::min(g, batch - c0);
     const char* src = static_cast<const char*>(in) + c0 * n * cb_;
@@ -450,7 +526,7 @@ void BigCore::exec(const void* in, void* out, void* work, long long batch, bool 
       a.in_dist = idist;
       a.out_dist = m;
       a.ncols = n2;
-      launch_pass(true, mode, ca, ga, a, f, (unsigned)(cnt * a.tiles_per_tr), cnt * m, s, library_only);
+      launch_pass(true, mode, ca, ga, a, f, (unsigned)(cnt * a.tiles_per_tr), cnt * m, s, library_only, opts.jit, tc);
     };
     auto pass_b = [&](int mode, const void* i, void* o, long long odist, int bk) {
       KArgs a{};
@@ -466,7 +542,7 @@ void BigCore::exec(const void* in, void* out, void* work, long long batch, bool 
       a.in_dist = m;
       a.out_dist = odist;
       a.ncols = n2;
-      launch_pass(false, mode, cb, gb, a, f, (unsigned)(cnt * a.tiles_per_tr), cnt * m, s, library_only);
+      launch_pass(false, mode, cb, gb, a, f, (unsigned)(cnt * a.tiles_per_tr), cnt * m, s, library_only, opts.jit, tc);
     };
     if (!blue) {
       pass_a(0, src, n, tmp, scale, back);

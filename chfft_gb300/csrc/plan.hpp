@@ -59,9 +59,9 @@ struct Smooth {
 };
 Smooth factor_smooth(long long n);
 
-// Stage list for a 7-smooth n (fewest passes; radices 16/8/4/2/10/5/3/7).
-// Returns false when n is not 7-smooth.
-bool make_stages(long long n, StageList* out);
+// Stage list for a 7-smooth n (fewest passes; radices 16/8/4/2/10/5/3/7,
+// and 32 when max_radix is 32). Returns false when n is not 7-smooth.
+bool make_stages(long long n, StageList* out, int max_radix = 16);
 // Threads a CTA needs to run `tpb` sequences with these stages (k1: one
 // butterfly per thread per pass; otherwise up to EPT/R per thread).
 int threads_needed(const StageList& st, int ept, int tpb, bool k1 = false);
@@ -71,18 +71,41 @@ bool fits_cta(const StageList& st, int dtype);
 // canonical order when the list has fewer than two passes.
 std::vector<int> pass_order(const StageList& st);
 
+// Tuning knobs of a plan: the autotuner's search space. Zero or -1 leaves a
+// knob to the built-in heuristic.
+struct PlanOpts {
+  int k1 = -1;           // one butterfly per thread (1), several (0), auto (-1)
+  int tpb = 0;           // sequences per CTA (rows), 0 auto
+  int max_radix = 0;     // specialised f32 kernels: 16 or 32 (0: 32)
+  int jit = -1;          // specialised kernels: policy (-1), never (0), always (1)
+  long long blue_m = 0;  // Bluestein length M (7-smooth, >= 2n - 1), 0 auto
+  int fs_n1 = 0;         // four-step column length n1, 0 auto
+  int fs_tpb = 0;        // four-step / 2-D column tile width, 0 auto
+  int l2_mb = 0;         // four-step chunk budget in MiB, 0 auto
+  int tc = 0;            // f32 radix-16 passes on tensor cores: 0 off, 1 FP16x2, 2 BF16x2, 3 BF16x3
+};
+
 // Complex core FFT of logical length n for one dtype: mixed radix when n is
-// 7-smooth and fits a CTA, otherwise Bluestein with a 7-smooth M >= 2n-1.
+// 7-smooth and fits a CTA, otherwise Bluestein with a 7-smooth M >= 2n-1
+// (blue_m when it is valid).
 struct Core {
   long long n = 0;
   int dtype = 0;
   bool blue = false;
   StageList st{};  // stages of the FFT actually run (length M for Bluestein)
-  DevBuf tw, chirp, bhat, stw;
-  bool build(long long n, int dtype, cudaStream_t s);  // false: unsupported size
+  // Radix-32 stage list for compile-time-stage kernels with 32 elements per
+  // thread (f32), with its own stage twiddles; wide.p is null when it equals st.
+  StageList sw{};
+  // Tensor-core pass order (r0, 16, ..., 16), n = r0 * 16^tc_s16 (f32, power
+  // of two), and its stage twiddles; tc_s16 = 0 when n does not qualify.
+  int tc_r0 = 0, tc_s16 = 0;
+  DevBuf tw, chirp, bhat, stw, wide, tcw;
+  bool build(long long n, int dtype, cudaStream_t s, long long blue_m = 0);  // false: unsupported size
+  void build_wide(cudaStream_t s);  // also the tensor-core pass order
+  void build_tc(cudaStream_t s);
   CoreDesc desc() const;
   long long fft_len() const { return st.n; }
-  size_t device_bytes() const { return tw.bytes + chirp.bytes + bhat.bytes + stw.bytes; }
+  size_t device_bytes() const { return tw.bytes + chirp.bytes + bhat.bytes + stw.bytes + wide.bytes + tcw.bytes; }
 };
 
 // Launch geometry of a CTA-per-`tpb`-sequences kernel.
@@ -90,17 +113,18 @@ struct Geo {
   int tpb = 1, threads = 32;
   size_t smem = 0;
   int ld = 0;
-  bool k1 = false;  // one-butterfly-per-thread kernel variant
+  bool k1 = false;     // one-butterfly-per-thread kernel variant
+  int max_radix = 32;  // compile-time-stage kernels: 32 allows the core's radix-32 list
 };
-Geo row_geo(const Core& c, long long count, int target_threads = 256);
-Geo col_geo(const Core& c, int ncols);
+Geo row_geo(const Core& c, long long count, const PlanOpts& o = PlanOpts{});
+Geo col_geo(const Core& c, int ncols, int tpb_opt = 0, const PlanOpts& o = PlanOpts{});
 
 // Smallest 7-smooth M >= lo that the CTA engine runs cheapest (M * passes).
 long long bluestein_length(long long n, int dtype);
 
 // Whether plan-time specialised kernels are used for a launch of `elems`
-// elements (CHFFT_JIT policy).
-bool want_specialised(long long elems);
+// elements (CHFFT_JIT policy, unless the plan's jit knob overrides it).
+bool want_specialised(long long elems, int jit_opt = -1);
 
 // Complex FFT of a length beyond one CTA: four-step N = n1 * n2 (column
 // pass + transposing row pass, jit/library kernels), or Bluestein with a
@@ -110,10 +134,11 @@ struct BigCore {
   long long m = 0;  // FFT length run (n, or the Bluestein M)
   int dtype = 0;
   bool blue = false;
-  int n1 = 0, n2 = 0, tw_l = 0;
+  int n1 = 0, n2 = 0, tw_l = 0, tw_shift = 0;
   Core ca, cb;  // column core (n1), row core (n2)
   DevBuf lo, hi, chirp, bhat;
-  bool build(long long n, int dtype, cudaStream_t s);  // false: unsupported
+  PlanOpts opts;
+  bool build(long long n, int dtype, cudaStream_t s, const PlanOpts& o = PlanOpts{});  // false: unsupported
   FourStep fs() const;
   long long chunk(long long batch) const;                  // transforms per chunk
   long long work_elems(long long batch) const;             // complex workspace elements
@@ -131,5 +156,11 @@ struct BigCore {
 
 // Split of a 7-smooth m into n1 x n2 CTA-sized factors (false if none).
 bool four_step_split(long long m, int dtype, int* n1, int* n2);
+// Smallest s with (2^s)^2 >= m: the inter-pass twiddle split w^e = hi[e >> s] lo[e & (2^s - 1)].
+inline int tw_shift_for(long long m) {
+  int s = 0;
+  while ((1LL << (2 * s)) < m) s++;
+  return s;
+}
 
 }  // namespace chfft

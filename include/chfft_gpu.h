@@ -220,6 +220,72 @@ typedef struct chfft_plan_info {
 
 CHFFT_API int chfft_plan_get_info(chfft_plan plan, chfft_plan_info* info);
 
+/* ---- tuning (no reference counterpart) -----------------------------------
+ * chfft fixes one plan per length: the factor order of
+ * src/prime_factorization.rs:66-113 and the Chirp-Z length of
+ * src/cfft1d.rs:114-140. Here the launch structure of a plan has knobs, an
+ * exhaustive autotuner times them, and a learned cost model (a 3-layer MLP
+ * trained on the GPU) proposes them for lengths it has not timed. A knob at
+ * -1 / 0 is left to the built-in heuristic. */
+typedef struct chfft_plan_config {
+  int k1;                  /* 1: one butterfly per thread and pass, 0: several, -1 auto */
+  int seq_per_cta;         /* sequences per CTA of the row kernels, 0 auto */
+  int max_radix;           /* f32 plan-time kernels: 16 or 32, 0 auto (32) */
+  int jit;                 /* plan-time specialised kernels: 1 always, 0 never, -1 policy (CHFFT_JIT) */
+  long long bluestein_len; /* Bluestein convolution length M (7-smooth, >= 2N-1), 0 auto */
+  int fs_n1;               /* four-step column length n1 (n1 | N), 0 auto */
+  int tile_cols;           /* four-step and 2-D column tile width, 0 auto */
+  int l2_chunk_mb;         /* four-step chunk budget in MiB, 0 auto (64) */
+  int tc_precision;        /* f32 radix-16 passes on the tensor cores (power-of-two CFft1D
+                              lengths >= 16, plan-time compiled): 0 off (FP32 cores),
+                              1 FP16 hi+lo, 2 BF16 hi+lo, 3 BF16 hi+mid+lo; FP32 accumulation */
+} chfft_plan_config;
+
+CHFFT_API void chfft_plan_config_default(chfft_plan_config* cfg);
+/* Applies cfg (rebuilding the plan's tables when the Bluestein length or the
+ * four-step split changes). Knobs a plan cannot use are ignored; invalid
+ * values fall back to the heuristic. */
+CHFFT_API int chfft_plan_set_config(chfft_plan plan, const chfft_plan_config* cfg);
+CHFFT_API int chfft_plan_get_config(chfft_plan plan, chfft_plan_config* cfg);
+/* The autotuner's search space for `batch` transforms: up to cap configs into
+ * out, their number into *n. tune_jit != 0 adds the jit / max_radix knobs. */
+CHFFT_API int chfft_plan_candidates(chfft_plan plan, size_t batch, int tune_jit, chfft_plan_config* out, int cap,
+                                    int* n);
+/* Cost-model features of (plan, batch, cfg): CHFFT_FEATURES floats. */
+#define CHFFT_FEATURES 40
+CHFFT_API int chfft_plan_features(chfft_plan plan, size_t batch, const chfft_plan_config* cfg, float* out);
+/* Exhaustive autotune: times every candidate (the method on `batch`
+ * transforms of device scratch data, median of `reps` launches after one
+ * warm-up), leaves the plan on the fastest, and reports each candidate and
+ * its milliseconds (up to cap) plus the index of the best. */
+CHFFT_API int chfft_autotune(chfft_plan plan, int method, size_t batch, int reps, int tune_jit,
+                             chfft_plan_config* cfgs, float* ms, int cap, int* n, int* best);
+
+/* Learned cost model: an MLP CHFFT_FEATURES -> hidden -> hidden -> 1 (ReLU,
+ * FP32) predicting log milliseconds, trained with Adam by this library's own
+ * CUDA forward / backward kernels. Inputs are standardised with the training
+ * set's moments, kept in the model. */
+typedef struct chfft_mlp_s* chfft_mlp;
+CHFFT_API int chfft_mlp_create(int hidden, unsigned seed, chfft_mlp* out);
+CHFFT_API int chfft_mlp_destroy(chfft_mlp m);
+CHFFT_API int chfft_mlp_num_params(chfft_mlp m);
+/* Parameters, flat: W1 (hidden x F), b1, W2 (hidden x hidden), b2, W3 (hidden), b3. */
+CHFFT_API int chfft_mlp_get_params(chfft_mlp m, float* out);
+CHFFT_API int chfft_mlp_set_params(chfft_mlp m, const float* p);
+/* Feature / target moments used to standardise (F means, F stds, target mean, target std). */
+CHFFT_API int chfft_mlp_set_moments(chfft_mlp m, const float* mean, const float* std, float y_mean, float y_std);
+CHFFT_API int chfft_mlp_get_moments(chfft_mlp m, float* mean, float* std, float* y_mean, float* y_std);
+/* Loss 0.5 * mean((f(x) - y)^2) over standardised rows and its gradient
+ * (num_params floats) from the GPU kernels: the quantity a gradient check
+ * compares. X is n x CHFFT_FEATURES raw features, y raw log ms. */
+CHFFT_API int chfft_mlp_loss_grad(chfft_mlp m, const float* X, const float* y, int n, float* loss, float* grad);
+/* Computes the moments from (X, y), then runs `epochs` of mini-batch Adam. */
+CHFFT_API int chfft_mlp_train(chfft_mlp m, const float* X, const float* y, int n, int epochs, int batch, float lr,
+                              unsigned seed, float* final_loss);
+CHFFT_API int chfft_mlp_predict(chfft_mlp m, const float* X, int n, float* y);
+/* Picks the candidate with the lowest predicted time and applies it. */
+CHFFT_API int chfft_plan_propose(chfft_plan plan, size_t batch, chfft_mlp m, int tune_jit, chfft_plan_config* chosen);
+
 /* ---- index arithmetic (bit-exact with the reference's plan code) -------- */
 
 /* prime_factorization(len, max) (src/prime_factorization.rs:66-113):
