@@ -9,40 +9,38 @@
 // matrices along K, `sbo` between groups of 8 rows.
 #pragma once
 
-#include <cstdint>
-
 namespace chfft {
 namespace tc {
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
 }
 
 // Byte offset of element (row, k) of a K-major 16-bit tile with K elements
 // per row in the canonical layout (lbo = 128, sbo = K * 16).
-__host__ __device__ constexpr uint32_t kmajor_offset(int row, int k, int K) {
-  return (uint32_t)((row >> 3) * (K * 16) + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+__host__ __device__ constexpr unsigned kmajor_offset(int row, int k, int K) {
+  return (unsigned)((row >> 3) * (K * 16) + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
 }
 
 // Shared-memory matrix descriptor (no swizzle, base offset 0).
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = 0;
-  d |= (uint64_t)((addr >> 4) & 0x3FFFu);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-  d |= (uint64_t)1 << 46;  // descriptor version of the sm_100 family
+__device__ __forceinline__ unsigned long long smem_desc(unsigned addr, unsigned lbo, unsigned sbo) {
+  unsigned long long d = 0;
+  d |= (unsigned long long)((addr >> 4) & 0x3FFFu);
+  d |= (unsigned long long)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (unsigned long long)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (unsigned long long)1 << 46;  // descriptor version of the sm_100 family
   return d;
 }
 
 // Instruction descriptor of kind::f16: FP32 accumulator, A and B both FP16
 // (or both BF16), both K-major, shape M x N.
-__host__ __device__ constexpr uint32_t idesc_f16(int M, int N, bool bf16) {
-  return (1u << 4) | ((bf16 ? 1u : 0u) << 7) | ((bf16 ? 1u : 0u) << 10) | ((uint32_t)(N >> 3) << 17) |
-         ((uint32_t)(M >> 4) << 24);
+__host__ __device__ constexpr unsigned idesc_f16(int M, int N, bool bf16) {
+  return (1u << 4) | ((bf16 ? 1u : 0u) << 7) | ((bf16 ? 1u : 0u) << 10) | ((unsigned)(N >> 3) << 17) |
+         ((unsigned)(M >> 4) << 24);
 }
 
 // D[tmem] (+)= A[smem] * B[smem]^T, one thread issues.
-__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+__device__ __forceinline__ void mma_f16(unsigned d_tmem, unsigned long long a, unsigned long long b, unsigned idesc, unsigned accumulate) {
   asm volatile(
       "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
@@ -50,20 +48,20 @@ __device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b,
 }
 
 // Arrives once on the mbarrier when every MMA this thread issued so far is done.
-__device__ __forceinline__ void commit(uint64_t* mbar) {
+__device__ __forceinline__ void commit(unsigned long long* mbar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(mbar))
                : "memory");
 }
 
 // Whole warp: allocate ncols (power of two >= 32) tensor-memory columns; the
 // address lands in *slot (shared memory).
-__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
+__device__ __forceinline__ void tmem_alloc(unsigned* slot, unsigned ncols) {
   asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)), "r"(ncols)
                : "memory");
   asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
 }
 
-__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+__device__ __forceinline__ void tmem_dealloc(unsigned taddr, unsigned ncols) {
   asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
 }
 
@@ -72,12 +70,12 @@ __device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence
 // Generic-proxy shared-memory writes become visible to the tensor core.
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+__device__ __forceinline__ void mbar_init(unsigned long long* b, unsigned count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
 }
 
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, uint32_t phase) {
-  uint32_t ok;
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned phase) {
+  unsigned ok;
   asm volatile(
       "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
       : "=r"(ok)
@@ -87,7 +85,7 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* b, uint32_t phase) {
 }
 
 // Bounded wait for phase `phase` of the mbarrier: false after `limit` polls.
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t phase, int limit) {
+__device__ __forceinline__ bool mbar_wait(unsigned long long* b, unsigned phase, int limit) {
   for (int i = 0; i < limit; i++) {
     if (mbar_try_wait(b, phase)) return true;
     __nanosleep(64);
@@ -97,8 +95,8 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t phase, int limit
 
 // This warp's 32 lanes x 32 consecutive FP32 columns starting at taddr
 // (lane field = 32 * (warp % 4)); thread i receives lane i.
-__device__ __forceinline__ void tmem_ld_32x32(uint32_t taddr, float* v) {
-  uint32_t r[32];
+__device__ __forceinline__ void tmem_ld_32x32(unsigned taddr, float* v) {
+  unsigned r[32];
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
       "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"

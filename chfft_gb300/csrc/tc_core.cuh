@@ -32,29 +32,29 @@ namespace chfft {
 
 namespace tcd {
 
-__device__ __forceinline__ uint32_t pack_f16x2(float lo_elem, float hi_elem) {
-  uint32_t r;
+__device__ __forceinline__ unsigned pack_f16x2(float lo_elem, float hi_elem) {
+  unsigned r;
   asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi_elem), "f"(lo_elem));
   return r;
 }
-__device__ __forceinline__ void unpack_f16x2(uint32_t v, float& a, float& b) {
+__device__ __forceinline__ void unpack_f16x2(unsigned v, float& a, float& b) {
   asm("{\n.reg .b16 l, h;\nmov.b32 {l, h}, %2;\ncvt.f32.f16 %0, l;\ncvt.f32.f16 %1, h;\n}\n"
       : "=f"(a), "=f"(b)
       : "r"(v));
 }
-__device__ __forceinline__ uint32_t pack_bf16x2(float lo_elem, float hi_elem) {
-  uint32_t r;
+__device__ __forceinline__ unsigned pack_bf16x2(float lo_elem, float hi_elem) {
+  unsigned r;
   asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi_elem), "f"(lo_elem));
   return r;
 }
-__device__ __forceinline__ void unpack_bf16x2(uint32_t v, float& a, float& b) {
+__device__ __forceinline__ void unpack_bf16x2(unsigned v, float& a, float& b) {
   a = __uint_as_float(v << 16);
   b = __uint_as_float(v & 0xFFFF0000u);
 }
 
 // Splits the pair (x0, x1) into NPART packed 16-bit parts, largest first.
 template <int PREC>
-__device__ __forceinline__ void split_pair(float x0, float x1, uint32_t* parts) {
+__device__ __forceinline__ void split_pair(float x0, float x1, unsigned* parts) {
   constexpr int NP = PREC == 3 ? 3 : 2;
 #pragma unroll
   for (int q = 0; q < NP; q++) {
@@ -73,6 +73,20 @@ __device__ __forceinline__ void split_pair(float x0, float x1, uint32_t* parts) 
 
 // 2^k as a float for |k| < 126.
 __device__ __forceinline__ float pow2f(int k) { return __int_as_float((127 + k) << 23); }
+
+// cos / sin of 2 pi m / 16, evaluated in double at compile time, rounded once.
+struct Dft16 {
+  float c[16], s[16];
+};
+__host__ __device__ constexpr Dft16 make_dft16() {
+  Dft16 t{};
+  for (int m = 0; m < 16; m++) {
+    t.c[m] = (float)ct::cos2pi(m, 16);
+    t.s[m] = (float)ct::sin2pi(m, 16);
+  }
+  return t;
+}
+__device__ constexpr Dft16 kDft16 = make_dft16();
 
 }  // namespace tcd
 
@@ -113,13 +127,13 @@ struct TcCore {
     const int t = row >> 7, r = row & 127;
 #pragma unroll
     for (int kb = 0; kb < 4; kb++) {
-      uint32_t w[NP][4];
+      unsigned w[NP][4];
 #pragma unroll
       for (int e = 0; e < 4; e++) {
         const int k = kb * 8 + 2 * e;
         const float x0 = k < 16 ? re[k] : im[k - 16];
         const float x1 = k < 16 ? re[k + 1] : im[k - 15];
-        uint32_t parts[NP];
+        unsigned parts[NP];
         tcd::split_pair<PREC>(x0, x1, parts);
 #pragma unroll
         for (int q = 0; q < NP; q++) w[q][e] = parts[q];
@@ -133,7 +147,7 @@ struct TcCore {
   }
 
   // The DFT-16 matrix B (32 x 32, row n' = output component, K = input
-  // component) in NP parts, from exact FP64 values.
+  // component) in NP parts, from FP64 values rounded once.
   __device__ __forceinline__ static void build_b(unsigned char* sb) {
     for (int i = threadIdx.x; i < 32 * 16; i += blockDim.x) {
       const int n = i / 16, kp = i % 16;  // kp: pair of K entries (2 kp, 2 kp + 1)
@@ -142,17 +156,16 @@ struct TcCore {
       for (int h = 0; h < 2; h++) {
         const int k = 2 * kp + h;
         const int j = n & 15, kk = k & 15;
-        double s, c;
-        sincospi((double)((j * kk) & 15) / 8.0, &s, &c);
+        const float c = tcd::kDft16.c[(j * kk) & 15], s = tcd::kDft16.s[(j * kk) & 15];
         const bool re_out = n < 16, re_in = k < 16;
         // Re Y = C a + S b; Im Y = -S a + C b (forward, w = exp(-2 pi i / 16)).
         v[h] = (float)(re_out ? (re_in ? c : s) : (re_in ? -s : c));
       }
-      uint32_t parts[NP];
+      unsigned parts[NP];
       tcd::split_pair<PREC>(v[0], v[1], parts);
 #pragma unroll
       for (int q = 0; q < NP; q++)
-        *reinterpret_cast<uint32_t*>(sb + q * (32 * 64) + tc::kmajor_offset(n, 2 * kp, 32)) = parts[q];
+        *reinterpret_cast<unsigned*>(sb + q * (32 * 64) + tc::kmajor_offset(n, 2 * kp, 32)) = parts[q];
     }
   }
 
@@ -163,8 +176,8 @@ struct TcCore {
     unsigned char* base = reinterpret_cast<unsigned char*>(sm.s);
     unsigned char* sa = base + A_OFF;
     unsigned char* sb = base + B_OFF;
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(base + BAR_OFF);
-    uint32_t* slot = reinterpret_cast<uint32_t*>(base + BAR_OFF + 8);
+    unsigned long long* mbar = reinterpret_cast<unsigned long long*>(base + BAR_OFF);
+    unsigned* slot = reinterpret_cast<unsigned*>(base + BAR_OFF + 8);
     int* timed_out = reinterpret_cast<int*>(base + BAR_OFF + 12);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const C* stw = static_cast<const C*>(d.stw);
@@ -186,7 +199,7 @@ struct TcCore {
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    const uint32_t tmem = *slot;
+    const unsigned tmem = *slot;
     constexpr int NB = N / 16;
     constexpr int ROW_ITERS = (ROWS + kTcThreads - 1) / kTcThreads;  // row slots per thread
     bool ok = true;
@@ -229,8 +242,8 @@ struct TcCore {
       __syncthreads();
       tc::fence_after_sync();
       if (tid == 0) {
-        constexpr uint32_t id = tc::idesc_f16(128, 32, PREC != 1);
-        const uint32_t a0 = tc::smem_u32(sa), b0 = tc::smem_u32(sb);
+        constexpr unsigned id = tc::idesc_f16(128, 32, PREC != 1);
+        const unsigned a0 = tc::smem_u32(sa), b0 = tc::smem_u32(sb);
         // Products (A part, B part) above the 2^-24 level, largest first.
         constexpr int pa[6] = {0, 1, 0, 1, 0, 2};
         constexpr int pb[6] = {0, 0, 1, 1, 2, 0};
@@ -240,8 +253,8 @@ struct TcCore {
             const int qa = PREC == 3 ? pa[p] : (p == 0 ? 0 : p == 1 ? 1 : 0);
             const int qb = PREC == 3 ? pb[p] : (p == 2 ? 1 : 0);
             for (int ks = 0; ks < 2; ks++) {
-              const uint64_t da = tc::smem_desc(a0 + (t * NP + qa) * (128 * 64) + ks * 256, 128, 512);
-              const uint64_t db = tc::smem_desc(b0 + qb * (32 * 64) + ks * 256, 128, 512);
+              const unsigned long long da = tc::smem_desc(a0 + (t * NP + qa) * (128 * 64) + ks * 256, 128, 512);
+              const unsigned long long db = tc::smem_desc(b0 + qb * (32 * 64) + ks * 256, 128, 512);
               tc::mma_f16(tmem + 32 * t, da, db, id, acc);
               acc = 1;
             }
@@ -264,7 +277,7 @@ struct TcCore {
         if (t >= T) continue;
         const int row = 128 * t + 32 * (warp & 3) + lane;
         float y[32];
-        tc::tmem_ld_32x32(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + 32 * t, y);
+        tc::tmem_ld_32x32(tmem + ((unsigned)(32 * (warp & 3)) << 16) + 32 * t, y);
         const int seq = row / NB, j = row - seq * NB;
         const int jm = j % Ns;
         const int bse = (j - jm) * 16 + jm;
