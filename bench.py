@@ -546,6 +546,8 @@ def run_large(args):
     stream = torch.cuda.current_stream(dev)
     sptr = stream.cuda_stream
     parts = [("c2c_2^20x64", 1 << 20, 64), ("c2c_4096x16384", 4096, 16384)]
+    if args.small:  # the profiling case: the same kernels on 128 / 256 MiB inputs
+        parts = [("c2c_2^20x16", 1 << 20, 16), ("c2c_4096x8192", 4096, 8192)]
     rng = np.random.default_rng(4)
     plans, d_in, d_out, h_in, h_out = [], [], [], [], []
     worst = 0.0
@@ -624,7 +626,7 @@ def run_large(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic N(0,1) complex with 1% of entries x1e3 (seeded)",
-        "config": {"workload": "cfft1d f32 N=2^20 x 64 + cfft1d f32 N=4096 x 16384, forward, plain FP32 path",
+        "config": {"workload": " + ".join(f"cfft1d f32 N={n} x {b}" for _, n, b in parts) + ", forward, plain FP32 path",
                    "l2": "inputs larger than L2 (512 MiB per part)"},
         "hbm_gbs": round(nbytes / (ms * 1e-3) / 1e9, 1),
         "parts": {name: {"ms": round(t, 4), "gbs": round(16.0 * n * b / (t * 1e-3) / 1e9, 1),
@@ -709,6 +711,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--small", action="store_true",
+                    help="large workload only: the same kernels at 1/4 and 1/2 the batch (profiling case)")
     ap.add_argument("--workload", choices=["batch", "large", "uneven", "costmodel"], default="batch",
                     help="batch: the headline configuration (default); large / uneven / costmodel: the others")
     args = ap.parse_args()

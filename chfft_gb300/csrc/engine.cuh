@@ -315,6 +315,7 @@ template <bool BLUE, bool TMINOR, bool FUSED, bool K1>
 struct DynCore {
   static constexpr bool kK1 = K1;
   static constexpr bool kStatic = false;
+  static constexpr int kMinBlocks = K1 ? 2 : 1;  // launch bounds: resident CTAs per SM
   // The kernel's shared-memory tile (layout shared with the kernel's own
   // pre-/post-phases).
   template <typename C>
@@ -334,16 +335,19 @@ struct DynCore {
 // threads along each sequence (coalesced loads of contiguous rows) whatever
 // TMINOR says for the others; any mapping of a pass's butterflies to threads
 // computes the same transform.
-template <int N, int TPB, int LD, int P, bool TMINOR, bool K1, int NS, int OFF, bool ROWS_FIRST, int R, int... Rest,
-          typename C, class Ld, class St>
+// EPT > 0 (with K1 false) gives every thread EPT / R butterflies of a
+// radix-R pass: EPT = the largest radix keeps every thread busy in every
+// pass of a mixed-radix list.
+template <int N, int TPB, int LD, int P, bool TMINOR, bool K1, int EPT, int NS, int OFF, bool ROWS_FIRST, int R,
+          int... Rest, typename C, class Ld, class St>
 __device__ __forceinline__ void static_passes(const C* stw, C* s, const Ld& ld, const St& st) {
   constexpr bool kMinor = TMINOR && !(ROWS_FIRST && OFF == 0);
   if constexpr (sizeof...(Rest) == 0) {
-    pass_body<R, kMinor, K1, true>(N, NS, TPB, stw + OFF, ld, st);
+    pass_body<R, kMinor, K1, true, EPT>(N, NS, TPB, stw + OFF, ld, st);
   } else {
     const SmemIO<C, P> sm{s, LD};
-    pass_body<R, kMinor, K1, true>(N, NS, TPB, stw + OFF, ld, sm);
-    static_passes<N, TPB, LD, P, TMINOR, K1, NS * R, OFF + (R - 1) * NS, ROWS_FIRST, Rest...>(stw, s, sm, st);
+    pass_body<R, kMinor, K1, true, EPT>(N, NS, TPB, stw + OFF, ld, sm);
+    static_passes<N, TPB, LD, P, TMINOR, K1, EPT, NS * R, OFF + (R - 1) * NS, ROWS_FIRST, Rest...>(stw, s, sm, st);
   }
 }
 
@@ -358,10 +362,14 @@ struct SpectrumStore {
   }
 };
 
-template <bool BLUE, bool TMINOR, bool K1, int M, int NU, int TPB, int LD, int P, int... Rs>
+// MINB: the resident CTAs per SM the kernel's launch bounds ask for (the
+// register budget follows from it); EPT: elements per thread of the
+// several-butterflies variant (0: the dtype's default).
+template <bool BLUE, bool TMINOR, bool K1, int M, int NU, int TPB, int LD, int P, int MINB, int EPT, int... Rs>
 struct StatCore {
   static constexpr bool kK1 = K1;
   static constexpr bool kStatic = true;
+  static constexpr int kMinBlocks = MINB;
   template <typename C>
   __device__ __forceinline__ static SmemIO<C, P> tile(unsigned char* base, int) {
     return SmemIO<C, P>{reinterpret_cast<C*>(base), LD};
@@ -373,14 +381,14 @@ struct StatCore {
                                              const St& st) {
     const C* stw = static_cast<const C*>(d.stw);
     if constexpr (!BLUE) {
-      static_passes<M, TPB, LD, P, TMINOR, K1, 1, 0, ROWS_FIRST, Rs...>(stw, sm.s, ld, st);
+      static_passes<M, TPB, LD, P, TMINOR, K1, EPT, 1, 0, ROWS_FIRST, Rs...>(stw, sm.s, ld, st);
     } else {
       const C* chirp = static_cast<const C*>(d.chirp);
       ChirpIn<C, Ld> l1{ld, chirp, NU};
       ChirpOut<C, St> s2{st, chirp, NU};
       SpectrumStore<C, SmemIO<C, P>> spec{sm, static_cast<const C*>(d.bhat)};
-      static_passes<M, TPB, LD, P, TMINOR, K1, 1, 0, ROWS_FIRST, Rs...>(stw, sm.s, l1, spec);
-      static_passes<M, TPB, LD, P, TMINOR, K1, 1, 0, false, Rs...>(stw, sm.s, sm, s2);
+      static_passes<M, TPB, LD, P, TMINOR, K1, EPT, 1, 0, ROWS_FIRST, Rs...>(stw, sm.s, l1, spec);
+      static_passes<M, TPB, LD, P, TMINOR, K1, EPT, 1, 0, false, Rs...>(stw, sm.s, sm, s2);
     }
   }
 };

@@ -155,8 +155,9 @@ std::string name_expression(Kernel k, int dtype, const Core& c, const StageList&
   s += c.blue ? "true," : "false,";
   s += column_mapped(k) ? "true," : "false,";
   s += g.k1 ? "true," : "false,";
+  const int minb = g.min_blocks > 0 ? g.min_blocks : (g.k1 || g.ept > 0 ? 2 : 1);
   s += std::to_string(sl.n) + "," + std::to_string(c.n) + "," + std::to_string(g.tpb) + "," + std::to_string(g.ld) +
-       "," + std::to_string(pad_period(sl));
+       "," + std::to_string(pad_period(sl)) + "," + std::to_string(minb) + "," + std::to_string(g.k1 ? 0 : g.ept);
   for (int r : pass_order(sl)) s += "," + std::to_string(r);
   s += ">";
   if (four_step(k)) s += ", " + std::to_string(mode);
@@ -222,10 +223,28 @@ int jit_launch(Kernel k, int dtype, const Core& c, const Geo& g0, const KArgs& a
   if (!load_api()) return 1;
   if (!c.stw.p) return 1;
   // Stage list: the radix-32 one where every thread holds 32 elements.
-  const bool wide = !g0.k1 && g0.max_radix >= 32 && c.wide.p;
+  const bool wide = !g0.k1 && g0.ept == 0 && g0.max_radix >= 32 && c.wide.p;
   const StageList& sl = wide ? c.sw : c.st;
   // The specialised tile uses its own pad period, hence its own stride.
   Geo g = g0;
+  // Balanced variant of a one-butterfly-per-thread geometry whose radices
+  // differ: every thread takes maxR / R butterflies of a radix-R pass, so no
+  // thread idles through the passes of the largest radix.
+  if (g.k1 && g.balance != 0) {
+    int rmin = 1 << 30, rmax = 0;
+    for (int r : pass_order(sl)) {
+      rmin = std::min(rmin, r);
+      rmax = std::max(rmax, r);
+    }
+    bool divides = rmax > 0;
+    for (int r : pass_order(sl)) divides = divides && rmax % r == 0;
+    if (rmax > rmin && divides) {
+      g.k1 = false;
+      g.ept = rmax;
+      int th = threads_needed(sl, rmax, g.tpb, false);
+      g.threads = std::max(32, ((th + 31) / 32) * 32);
+    }
+  }
   g.ld = tile_ld(sl, g.tpb, dtype, column_mapped(k));
   g.smem = (size_t)g.tpb * g.ld * cplx_bytes(dtype);
   if (g.smem > kMaxSmem) return 1;

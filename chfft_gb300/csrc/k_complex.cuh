@@ -42,7 +42,7 @@ struct RowStore {
 };
 
 template <typename T, class CoreT>
-__global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_c2c(const KArgs a) {
+__global__ void __launch_bounds__(kMaxThreads, CoreT::kMinBlocks) k_c2c(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
@@ -81,7 +81,7 @@ struct ColStore {
 };
 
 template <typename T, class CoreT>
-__global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_cols(const KArgs a) {
+__global__ void __launch_bounds__(kMaxThreads, CoreT::kMinBlocks) k_cols(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
@@ -140,7 +140,7 @@ struct ColsAStore {
 };
 
 template <typename T, class CoreT, int MODE>
-__global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_cols_tw(const KArgs a, const FourStep fs) {
+__global__ void __launch_bounds__(kMaxThreads, CoreT::kMinBlocks) k_cols_tw(const KArgs a, const FourStep fs) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
@@ -188,7 +188,7 @@ struct RowsBLoad {
 };
 
 template <typename T, class CoreT, int MODE>
-__global__ void __launch_bounds__(kMaxThreads, CoreT::kK1 ? 2 : 1) k_rows_t(const KArgs a, const FourStep fs) {
+__global__ void __launch_bounds__(kMaxThreads, CoreT::kMinBlocks) k_rows_t(const KArgs a, const FourStep fs) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const auto sm = CoreT::template tile<C>(smem_raw, a.ld);

@@ -301,6 +301,8 @@ static void fft_f64_inplace(double2* d_data, const Core& c64, cudaStream_t s) {
 Geo row_geo(const Core& c, long long count, const PlanOpts& o) {
   Geo g;
   g.max_radix = o.max_radix == 16 ? 16 : 32;
+  g.min_blocks = o.min_blocks;
+  g.balance = o.balance;
   const int ept = ept_of(c.dtype);
   const int m = c.st.n;
   g.ld = smem_ld(m);
@@ -333,6 +335,8 @@ Geo row_geo(const Core& c, long long count, const PlanOpts& o) {
 Geo col_geo(const Core& c, int ncols, int tpb_opt, const PlanOpts& o) {
   Geo g;
   g.max_radix = o.max_radix == 16 ? 16 : 32;
+  g.min_blocks = o.min_blocks;
+  g.balance = o.balance;
   const int ept = ept_of(c.dtype);
   g.ld = smem_ld(c.st.n);
   const size_t per = (size_t)g.ld * cplx_bytes(c.dtype);

@@ -83,6 +83,8 @@ struct PlanOpts {
   int fs_tpb = 0;        // four-step / 2-D column tile width, 0 auto
   int l2_mb = 0;         // four-step chunk budget in MiB, 0 auto
   int tc = 0;            // f32 radix-16 passes on tensor cores: 0 off, 1 FP16x2, 2 BF16x2, 3 BF16x3
+  int min_blocks = 0;    // specialised kernels: launch-bounds CTAs per SM, 0 auto
+  int balance = -1;      // specialised kernels: balanced mixed-radix variant (-1 auto = on, 0 off, 1 on)
 };
 
 // Complex core FFT of logical length n for one dtype: mixed radix when n is
@@ -115,6 +117,9 @@ struct Geo {
   int ld = 0;
   bool k1 = false;     // one-butterfly-per-thread kernel variant
   int max_radix = 32;  // compile-time-stage kernels: 32 allows the core's radix-32 list
+  int min_blocks = 0;  // compile-time-stage kernels: launch-bounds CTAs per SM (0: 2 for k1, else 1)
+  int ept = 0;         // compile-time-stage kernels: elements per thread of the several-butterflies variant
+  int balance = -1;    // compile-time-stage kernels: balanced variant of a mixed-radix k1 geometry (-1 auto, 0 off)
 };
 Geo row_geo(const Core& c, long long count, const PlanOpts& o = PlanOpts{});
 Geo col_geo(const Core& c, int ncols, int tpb_opt = 0, const PlanOpts& o = PlanOpts{});

@@ -28,6 +28,8 @@ PlanOpts to_opts(const chfft_plan_config& c) {
   o.fs_tpb = c.tile_cols;
   o.l2_mb = c.l2_chunk_mb;
   o.tc = c.tc_precision;
+  o.min_blocks = c.min_blocks_per_sm;
+  o.balance = c.balanced;
   return o;
 }
 
@@ -42,6 +44,8 @@ chfft_plan_config to_cfg(const PlanOpts& o) {
   c.tile_cols = o.fs_tpb;
   c.l2_chunk_mb = o.l2_mb;
   c.tc_precision = o.tc;
+  c.min_blocks_per_sm = o.min_blocks;
+  c.balanced = o.balance;
   return c;
 }
 
@@ -72,8 +76,12 @@ struct Resolved {
   long long fft_len = 0, ctas = 0, chunks = 1, l2mb = 0;
   int cnt[kNumRadix] = {0};
   int npass = 0, rfirst = 0, rlast = 0;
+  int minb = 0;          // specialised kernels: launch-bounds CTAs per SM
+  bool balanced = false;  // specialised kernels: balanced mixed-radix variant
 
-  auto key() const { return std::make_tuple(big, blue, k1, jit, wide, tpb, tile, n1, fft_len, l2mb, chunks); }
+  auto key() const {
+    return std::make_tuple(big, blue, k1, jit, wide, tpb, tile, n1, fft_len, l2mb, chunks, minb, balanced);
+  }
 };
 
 void add_stages(Resolved& r, const StageList& st) {
@@ -124,6 +132,17 @@ Resolved resolve(const PlanImpl& p, long long batch, const PlanOpts& o) {
     r.threads = wide ? std::max(32, (threads_needed(e, ept_of(dt), g.tpb, false) + 31) / 32 * 32) : g.threads;
     r.smem = g.smem;
     r.ctas = (count + g.tpb - 1) / g.tpb;
+    r.minb = r.jit ? (o.min_blocks > 0 ? o.min_blocks : (g.k1 ? 2 : 1)) : 0;
+    if (r.jit && g.k1 && o.balance != 0) {
+      int rmin = 1 << 30, rmax = 0;
+      for (int x : pass_order(e)) {
+        rmin = std::min(rmin, x);
+        rmax = std::max(rmax, x);
+      }
+      bool divides = rmax > 0;
+      for (int x : pass_order(e)) divides = divides && rmax % x == 0;
+      r.balanced = rmax > rmin && divides;
+    }
     add_stages(r, e);
   };
   switch (p.kind) {
@@ -242,7 +261,7 @@ void features(const PlanImpl& p, long long batch, const PlanOpts& o, float* f) {
   f[k++] = (float)lg2((double)batch);
   f[k++] = (float)p.dtype;
   f[k++] = (float)p.kind;
-  f[k++] = r.k1 ? 1.f : 0.f;
+  f[k++] = r.balanced ? 0.5f : (r.k1 ? 1.f : 0.f);
   f[k++] = (float)lg2((double)r.tpb);
   f[k++] = (float)r.threads / kMaxThreads;
   f[k++] = (float)r.smem / (float)kMaxSmem;
@@ -260,6 +279,7 @@ void features(const PlanImpl& p, long long batch, const PlanOpts& o, float* f) {
   f[k++] = (float)lg2((double)r.l2mb);
   f[k++] = (float)lg2((double)len * (double)batch);
   f[k++] = (float)lg2((double)r.chunks);
+  f[k++] = (float)r.minb;
 }
 
 // Bluestein lengths to try: the cheapest M by the engine's cost rule and the
@@ -298,6 +318,14 @@ std::vector<PlanOpts> candidates(const PlanImpl& p, long long batch, bool tune_j
         o.k1 = 1;
         o.tpb = t;
         out.push_back(o);
+        if (o.jit == 1) {  // a tighter register budget for a third resident CTA; no balancing
+          PlanOpts q = o;
+          q.min_blocks = 3;
+          out.push_back(q);
+          q = o;
+          q.balance = 0;
+          out.push_back(q);
+        }
       }
     }
     for (int t : {1, 2, 4, 8}) {

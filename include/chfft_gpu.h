@@ -239,6 +239,11 @@ typedef struct chfft_plan_config {
   int tc_precision;        /* f32 radix-16 passes on the tensor cores (power-of-two CFft1D
                               lengths >= 16, plan-time compiled): 0 off (FP32 cores),
                               1 FP16 hi+lo, 2 BF16 hi+lo, 3 BF16 hi+mid+lo; FP32 accumulation */
+  int min_blocks_per_sm;   /* plan-time kernels: CTAs per SM their launch bounds target
+                              (the register budget), 0 auto */
+  int balanced;            /* plan-time kernels with mixed radices: 1 / -1 (auto) every thread
+                              takes maxR / R butterflies of a radix-R pass, 0 one butterfly per
+                              thread and pass (threads idle through the larger radices) */
 } chfft_plan_config;
 
 CHFFT_API void chfft_plan_config_default(chfft_plan_config* cfg);
