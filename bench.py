@@ -643,6 +643,85 @@ def run_large(args):
     return 0
 
 
+def run_f64(args):
+    """CFft1D<f64> forward + backward of one N = 1024 transform (latency):
+    device time on device pointers, end-to-end time through chfft_execute on
+    host arrays, relative L2 against the oracle's f64 output (<= 1e-12)."""
+    import torch
+
+    import chfft_gb300 as cg
+    import oracle
+
+    n = 1024
+    rng = np.random.default_rng(1)
+    x = (rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n)).astype(np.complex128)
+    plan = cg.CFft1D.with_len(n, np.float64)
+    ref_f = oracle.cfft1d(x, "forward")
+    ref_b = oracle.cfft1d(ref_f, "backward")
+    y = plan.forward(x)
+    z = plan.backward(y)
+    err_f = float(np.linalg.norm(y - ref_f) / np.linalg.norm(ref_f))
+    err_b = float(np.linalg.norm(z - ref_b) / np.linalg.norm(ref_b))
+    if max(err_f, err_b) > 1e-12:
+        raise SystemExit(f"f64 N=1024: rel-L2 {max(err_f, err_b):.2e} > 1e-12")
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+    d_x = torch.from_numpy(x.view(np.float64)).to(dev)
+    d_y = torch.empty_like(d_x)
+    d_z = torch.empty_like(d_x)
+
+    def step():
+        plan.execute_device("forward", d_x.data_ptr(), d_y.data_ptr(), 1, sp)
+        plan.execute_device("backward", d_y.data_ptr(), d_z.data_ptr(), 1, sp)
+
+    reps = max(args.steps, 200)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    evs = []
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step()
+        b.record(stream)
+        evs.append((a, b))
+    torch.cuda.synchronize()
+    dev_us = statistics.median(a.elapsed_time(b) for a, b in evs) * 1e3
+    e2e = []
+    for k in range(args.warmup + reps):
+        t0 = time.perf_counter()
+        yy = plan.forward(x)
+        plan.backward(yy)
+        if k >= args.warmup:
+            e2e.append(time.perf_counter() - t0)
+    e2e_us = statistics.median(e2e) * 1e6
+    cpu = []
+    for k in range(5 + reps):
+        _, t1 = oracle.cfft1d(x, "forward", timing=True)
+        _, t2 = oracle.cfft1d(ref_f, "backward", timing=True)
+        if k >= 5:
+            cpu.append(t1 + t2)
+    cpu_us = statistics.median(cpu) * 1e6
+    flops = 2 * 5.0 * n * math.log2(n)
+    line = {
+        "metric": METRIC, "value": round(flops / (dev_us * 1e-6) / 1e9, 3), "unit": "GFLOP/s", "n_gpus": 1,
+        "steps": reps, "warmup": args.warmup, "ms_per_step": round(dev_us / 1e3, 5), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic uniform[-1,1) complex, seed 1",
+        "config": {"workload": "cfft1d f64 N=1024, one transform, forward + backward (latency)",
+                   "l2": "resident (one 16 KiB transform)"},
+        "latency_us": {"device": round(dev_us, 2), "e2e_host_arrays": round(e2e_us, 2), "cpu_oracle_1_thread": round(cpu_us, 2)},
+        "rel_l2_vs_oracle_f64": {"forward": err_f, "backward": err_b},
+        "e2e": {"value": round(flops / (e2e_us * 1e-6) / 1e9, 3), "unit": "GFLOP/s",
+                "h2d_bytes_per_step": 2 * 16 * n, "d2h_bytes_per_step": 2 * 16 * n},
+        "cpu_baseline": {"value": round(flops / (cpu_us * 1e-6) / 1e9, 3), "unit": "GFLOP/s", "cores": 1, "kind": "port",
+                         "sample": "the same forward + backward of N=1024 f64 on one host thread"},
+        "gpu_launches": 2 * reps,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_costmodel(args):
     """Learned plan cost model: exhaustive autotune timings of seeded lengths
     (log-uniform in [64, 2^22]) at batches 1 / 64 / 4096 (capped at 2^24
@@ -713,8 +792,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true",
                     help="large workload only: the same kernels at 1/4 and 1/2 the batch (profiling case)")
-    ap.add_argument("--workload", choices=["batch", "large", "uneven", "costmodel"], default="batch",
-                    help="batch: the headline configuration (default); large / uneven / costmodel: the others")
+    ap.add_argument("--workload", choices=["batch", "large", "uneven", "costmodel", "f64"], default="batch",
+                    help="batch: the headline configuration (default); large / uneven / costmodel / f64: the others")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -728,6 +807,8 @@ def main():
         return run_large(args)
     if args.workload == "costmodel":
         return run_costmodel(args)
+    if args.workload == "f64":
+        return run_f64(args)
     if world > 1:
         import torch
 

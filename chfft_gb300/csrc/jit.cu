@@ -42,6 +42,7 @@ struct Api {
   CUresult (*cuLaunchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned,
                              CUstream, void**, void**) = nullptr;
   CUresult (*cuFuncSetAttribute)(CUfunction, int, int) = nullptr;
+  CUresult (*cuOccupancyMaxActiveBlocksPerMultiprocessor)(int*, CUfunction, int, size_t) = nullptr;
   nvrtcResult (*nvrtcCreateProgram)(nvrtcProgram*, const char*, const char*, int, const char* const*,
                                     const char* const*) = nullptr;
   nvrtcResult (*nvrtcAddNameExpression)(nvrtcProgram, const char*) = nullptr;
@@ -91,6 +92,7 @@ bool load_api() {
             sym(cu, "cuModuleGetFunction", &g_api.cuModuleGetFunction) &&
             sym(cu, "cuLaunchKernel", &g_api.cuLaunchKernel) &&
             sym(cu, "cuFuncSetAttribute", &g_api.cuFuncSetAttribute) &&
+            sym(cu, "cuOccupancyMaxActiveBlocksPerMultiprocessor", &g_api.cuOccupancyMaxActiveBlocksPerMultiprocessor) &&
             sym(rtc, "nvrtcCreateProgram", &g_api.nvrtcCreateProgram) &&
             sym(rtc, "nvrtcAddNameExpression", &g_api.nvrtcAddNameExpression) &&
             sym(rtc, "nvrtcCompileProgram", &g_api.nvrtcCompileProgram) &&
@@ -202,6 +204,15 @@ bool compile(const std::string& expr, Entry* e, std::string* log) {
 
 }  // namespace
 
+int num_sms() {
+  static int n[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return 1;
+  if (!n[dev]) cudaDeviceGetAttribute(&n[dev], cudaDevAttrMultiProcessorCount, dev);
+  return n[dev] > 0 ? n[dev] : 1;
+}
+
 JitMode jit_mode() {
   const char* v = std::getenv("CHFFT_JIT");
   if (!v || !*v || !std::strcmp(v, "auto")) return JitMode::AUTO;
@@ -276,6 +287,16 @@ int jit_launch(Kernel k, int dtype, const Core& c, const Geo& g0, const KArgs& a
   if ((int)g.smem > 48 * 1024 && e.smem_set < (int)g.smem) {
     if (g_api.cuFuncSetAttribute(e.fn, kAttrMaxDynSmem, (int)g.smem) != 0) return 2;
     e.smem_set = (int)g.smem;
+  }
+  // L2 prefetch of the next wave's input (rows, columns, four-step passes).
+  const bool prefetching = k == Kernel::C2C || k == Kernel::COLS || four_step(k);
+  a.ahead = 0;
+  if (prefetching && g.prefetch > 0) {
+    int per_sm = 0;
+    if (g_api.cuOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, e.fn, g.threads, g.smem) == 0 && per_sm > 0) {
+      const long long resident = (long long)per_sm * num_sms();
+      if (g.prefetch > 0 || (long long)blocks > resident) a.ahead = resident;
+    }
   }
   void* args[] = {const_cast<KArgs*>(&a), const_cast<FourStep*>(fs)};
   if (g_api.cuLaunchKernel(e.fn, blocks, 1, 1, g.threads, 1, 1, (unsigned)g.smem, (CUstream)stream, args, nullptr) != 0)

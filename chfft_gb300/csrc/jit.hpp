@@ -28,6 +28,8 @@ int jit_launch_tc(Kernel k, const Core& c, int prec, int tpb, const KArgs& a, un
 // qualify (row tiles of 128 radix-16 butterflies, at most 16 of them, and
 // the shared-memory limit). ld receives the tile stride.
 size_t tc_geometry(const Core& c, Kernel k, int tpb, int prec, int* ld);
+// Streaming multiprocessors of the current device.
+int num_sms();
 // Number of specialised kernels compiled in this process.
 size_t jit_cache_size();
 

@@ -11,6 +11,23 @@ namespace chfft {
 
 namespace kern {
 
+// L2 prefetch of a later CTA's input. A launch of more CTAs than fit the GPU
+// at once runs in waves; the CTA that starts on an SM when this one retires
+// is about `ahead` (the CTAs resident at once) blocks later, so each CTA asks
+// L2 for that tile's input lines (128-byte lines spread over its threads)
+// and the next wave's HBM reads overlap this wave's passes.
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+// `rows` runs of `bytes` bytes, `stride` bytes apart.
+__device__ __forceinline__ void prefetch_rows(const char* base, long long rows, long long bytes, long long stride) {
+  const long long lines = (bytes + 127) / 128;
+  for (long long i = threadIdx.x; i < rows * lines; i += blockDim.x) {
+    const long long r = i / lines, l = i - r * lines;
+    prefetch_l2(base + r * stride + l * 128);
+  }
+}
+
 // ---------------------------------------------------------------- rows
 // Contiguous sequences. The backward transform conjugates on the way in and
 // out (conj(F(conj x)) = F^-1 x up to scale), so one set of forward
@@ -46,6 +63,12 @@ __global__ void __launch_bounds__(kMaxThreads, CoreT::kMinBlocks) k_c2c(const KA
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
+  if (a.ahead > 0) {
+    const long long nx = (long long)blockIdx.x + a.ahead;
+    if (nx * a.tpb < a.count)
+      prefetch_rows((const char*)((const C*)a.in + nx * a.tpb * a.in_dist), min((long long)a.tpb, a.count - nx * a.tpb),
+                    (long long)a.core.n * sizeof(C), a.in_dist * (long long)sizeof(C));
+  }
   const long long t0 = (long long)blockIdx.x * a.tpb;
   const int nvalid = (int)min((long long)a.tpb, a.count - t0);
   RowLoad<C> ld{(const C*)a.in + t0 * a.in_dist, a.in_dist, nvalid, (T)a.scale, a.back};
@@ -85,6 +108,15 @@ __global__ void __launch_bounds__(kMaxThreads, CoreT::kMinBlocks) k_cols(const K
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
+  if (a.ahead > 0) {
+    const long long nx = (long long)blockIdx.x + a.ahead;
+    if (nx < a.count * a.tiles_per_tr) {
+      const long long ntr = nx / a.tiles_per_tr;
+      const int nc0 = (int)(nx - ntr * a.tiles_per_tr) * a.tpb;
+      prefetch_rows((const char*)((const C*)a.in + ntr * a.in_dist + nc0), a.core.n,
+                    (long long)min(a.tpb, a.ncols - nc0) * sizeof(C), (long long)a.ncols * sizeof(C));
+    }
+  }
   const long long tr = blockIdx.x / a.tiles_per_tr;
   const int c0 = (int)(blockIdx.x - tr * a.tiles_per_tr) * a.tpb;
   const int nvalid = min(a.tpb, a.ncols - c0);
@@ -101,41 +133,55 @@ __global__ void __launch_bounds__(kMaxThreads, CoreT::kMinBlocks) k_cols(const K
 // L a power of two so the split is a shift and a mask
 // (FourStep in kernels.cuh).
 
+// The four-step kernels' MODE template argument: bits 0-1 the pass mode,
+// bit 2 (kL2Hints) L2 eviction priorities: the intermediate is stored
+// evict_last so pass B can find it in L2, streamed data goes evict_first.
+constexpr int kL2Hints = 4;
+
 // Pass A loader: MODE 0 plain (scale, conjugate for backward); MODE 1 the
 // Bluestein input x_j c_j for flat index j = n1 N2 + n2 < n_user, else 0.
-template <typename C, int MODE>
+template <typename C, int MODE, bool HINTS>
 struct ColsALoad {
   const C* in;  // first column of the tile
   int ncols, nvalid, c0;
   typename Real<C>::type scale;
   int back;
   const FourStep* fs;
+  unsigned long long pol;  // L2 policy of the streamed input (HINTS)
+  __device__ __forceinline__ C get(long long k) const {
+    if constexpr (HINTS) return ld_policy(in + k, pol);
+    return in[k];
+  }
   __device__ __forceinline__ C load(int t, int i) const {
     if (t >= nvalid) return czero<C>();
     if (MODE == 1) {
       const long long j = (long long)i * ncols + c0 + t;
       if (j >= fs->n_user) return czero<C>();
-      C v = cscale(in[(long long)i * ncols + t], scale);
+      C v = cscale(get((long long)i * ncols + t), scale);
       if (back) v = cconj(v);
       return cmul(v, __ldg(&static_cast<const C*>(fs->chirp)[j]));
     }
-    C v = cscale(in[(long long)i * ncols + t], scale);
+    C v = cscale(get((long long)i * ncols + t), scale);
     return back ? cconj(v) : v;
   }
 };
 
-template <typename C>
+template <typename C, bool HINTS>
 struct ColsAStore {
   C* out;
   int ncols, nvalid, c0;
   const FourStep* fs;
+  unsigned long long pol;  // L2 policy of the intermediate (HINTS)
   __device__ __forceinline__ void store(int t, int k1, C v) const {
     if (t >= nvalid) return;
     const long long e = (long long)k1 * (c0 + t);  // < N
     const C* lo = static_cast<const C*>(fs->lo);
     const C* hi = static_cast<const C*>(fs->hi);
     const C w = cmul(__ldg(&hi[e >> fs->tw_shift]), __ldg(&lo[e & ((1LL << fs->tw_shift) - 1)]));
-    out[(long long)k1 * ncols + t] = cmul(v, w);
+    if constexpr (HINTS)
+      st_policy(out + (long long)k1 * ncols + t, cmul(v, w), pol);
+    else
+      out[(long long)k1 * ncols + t] = cmul(v, w);
   }
 };
 
@@ -144,11 +190,28 @@ __global__ void __launch_bounds__(kMaxThreads, CoreT::kMinBlocks) k_cols_tw(cons
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
+  if (a.ahead > 0) {
+    const long long nx = (long long)blockIdx.x + a.ahead;
+    if (nx < a.count * a.tiles_per_tr) {
+      const long long ntr = nx / a.tiles_per_tr;
+      const int nc0 = (int)(nx - ntr * a.tiles_per_tr) * a.tpb;
+      // MODE 1 reads flat indices below n_user only (the rest is zero padding).
+      const long long rows =
+          (MODE & 3) == 1 ? min((long long)fs.n1, (fs.n_user - nc0 + a.ncols - 1) / a.ncols) : fs.n1;
+      prefetch_rows((const char*)((const C*)a.in + ntr * a.in_dist + nc0), rows,
+                    (long long)min(a.tpb, a.ncols - nc0) * sizeof(C), (long long)a.ncols * sizeof(C));
+    }
+  }
   const long long tr = blockIdx.x / a.tiles_per_tr;
   const int c0 = (int)(blockIdx.x - tr * a.tiles_per_tr) * a.tpb;
   const int nvalid = min(a.tpb, a.ncols - c0);
-  ColsALoad<C, MODE> ld{(const C*)a.in + tr * a.in_dist + c0, a.ncols, nvalid, c0, (T)a.scale, a.back, &fs};
-  ColsAStore<C> st{(C*)a.out + tr * a.out_dist + c0, a.ncols, nvalid, c0, &fs};
+  // The input streams through L2 once; the intermediate should stay for pass B.
+  constexpr bool kHints = (MODE & kL2Hints) != 0;
+  const unsigned long long pin = kHints ? l2_evict_first() : 0ull;
+  const unsigned long long pout = kHints ? l2_evict_last() : 0ull;
+  ColsALoad<C, MODE & 3, kHints> ld{(const C*)a.in + tr * a.in_dist + c0, a.ncols, nvalid, c0, (T)a.scale, a.back,
+                                    &fs, pin};
+  ColsAStore<C, kHints> st{(C*)a.out + tr * a.out_dist + c0, a.ncols, nvalid, c0, &fs, pout};
   CoreT::run(a.core, a.tpb, sm, ld, st);
 }
 
@@ -157,33 +220,44 @@ __global__ void __launch_bounds__(kMaxThreads, CoreT::kMinBlocks) k_cols_tw(cons
 // MODE 1 Bluestein spectrum: conj(X_k B^_k), the inverse FFT's input;
 // MODE 2 Bluestein output: k < n_user gets conj(X_k) c_k (conjugated again
 // for backward).
-template <typename C, int MODE>
+template <typename C, int MODE, bool HINTS>
 struct RowsBStore {
   C* out;  // transform base
   int r0, nvalid, n1, back;
   const FourStep* fs;
+  unsigned long long pol;  // L2 policy of the output (HINTS)
+  __device__ __forceinline__ void put(long long k, C v) const {
+    if constexpr (HINTS)
+      st_policy(out + k, v, pol);
+    else
+      out[k] = v;
+  }
   __device__ __forceinline__ void store(int t, int k2, C v) const {
     if (t >= nvalid) return;
     const long long k = (long long)(r0 + t) + (long long)n1 * k2;
     if (MODE == 0) {
-      out[k] = back ? cconj(v) : v;
+      put(k, back ? cconj(v) : v);
     } else if (MODE == 1) {
-      out[k] = cconj(cmul(v, __ldg(&static_cast<const C*>(fs->bhat)[k])));
+      put(k, cconj(cmul(v, __ldg(&static_cast<const C*>(fs->bhat)[k]))));
     } else {
       if (k < fs->n_user) {
         C y = cmul(cconj(v), __ldg(&static_cast<const C*>(fs->chirp)[k]));
-        out[k] = back ? cconj(y) : y;
+        put(k, back ? cconj(y) : y);
       }
     }
   }
 };
 
-template <typename C>
+template <typename C, bool HINTS>
 struct RowsBLoad {
   const C* in;  // first row of the tile
   int n2, nvalid;
+  unsigned long long pol;  // the intermediate is read once more, then dropped first (HINTS)
   __device__ __forceinline__ C load(int t, int i) const {
-    return t < nvalid ? in[(long long)t * n2 + i] : czero<C>();
+    if (t >= nvalid) return czero<C>();
+    const long long k = (long long)t * n2 + i;
+    if constexpr (HINTS) return ld_policy(in + k, pol);
+    return in[k];
   }
 };
 
@@ -192,6 +266,15 @@ __global__ void __launch_bounds__(kMaxThreads, CoreT::kMinBlocks) k_rows_t(const
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
+  if (a.ahead > 0) {
+    const long long nx = (long long)blockIdx.x + a.ahead;
+    if (nx < a.count * a.tiles_per_tr) {
+      const long long ntr = nx / a.tiles_per_tr;
+      const int nr0 = (int)(nx - ntr * a.tiles_per_tr) * a.tpb;
+      prefetch_rows((const char*)((const C*)a.in + ntr * a.in_dist + (long long)nr0 * fs.n2), 1,
+                    (long long)min(a.tpb, fs.n1 - nr0) * fs.n2 * sizeof(C), 0);
+    }
+  }
   const long long tr = blockIdx.x / a.tiles_per_tr;
   const int r0 = (int)(blockIdx.x - tr * a.tiles_per_tr) * a.tpb;
   const int nvalid = min(a.tpb, fs.n1 - r0);
@@ -199,8 +282,12 @@ __global__ void __launch_bounds__(kMaxThreads, CoreT::kMinBlocks) k_rows_t(const
   // then run the FFT with consecutive threads across rows so the transposed
   // store is contiguous. Compile-time-stage cores fuse the row load into
   // their first pass; the others stage it through the tile.
-  RowsBLoad<C> rl{(const C*)a.in + tr * a.in_dist + (long long)r0 * fs.n2, fs.n2, nvalid};
-  RowsBStore<C, MODE> st{(C*)a.out + tr * a.out_dist, r0, nvalid, fs.n1, a.back, &fs};
+  // MODE 1 writes the next pass's input (kept in L2); otherwise the output streams out.
+  constexpr bool kHints = (MODE & kL2Hints) != 0;
+  const unsigned long long pin = kHints ? l2_evict_first() : 0ull;
+  const unsigned long long pout = kHints ? ((MODE & 3) == 1 ? l2_evict_last() : l2_evict_first()) : 0ull;
+  RowsBLoad<C, kHints> rl{(const C*)a.in + tr * a.in_dist + (long long)r0 * fs.n2, fs.n2, nvalid, pin};
+  RowsBStore<C, MODE & 3, kHints> st{(C*)a.out + tr * a.out_dist, r0, nvalid, fs.n1, a.back, &fs, pout};
   if constexpr (CoreT::kStatic) {
     CoreT::template run<true>(a.core, a.tpb, sm, rl, st);
   } else {

@@ -303,6 +303,7 @@ Geo row_geo(const Core& c, long long count, const PlanOpts& o) {
   g.max_radix = o.max_radix == 16 ? 16 : 32;
   g.min_blocks = o.min_blocks;
   g.balance = o.balance;
+  g.prefetch = o.prefetch;
   const int ept = ept_of(c.dtype);
   const int m = c.st.n;
   g.ld = smem_ld(m);
@@ -337,6 +338,7 @@ Geo col_geo(const Core& c, int ncols, int tpb_opt, const PlanOpts& o) {
   g.max_radix = o.max_radix == 16 ? 16 : 32;
   g.min_blocks = o.min_blocks;
   g.balance = o.balance;
+  g.prefetch = o.prefetch;
   const int ept = ept_of(c.dtype);
   g.ld = smem_ld(c.st.n);
   const size_t per = (size_t)g.ld * cplx_bytes(c.dtype);
@@ -381,14 +383,16 @@ bool four_step_split(long long m, int dtype, int* n1, int* n2) {
 
 static void launch_pass(bool pass_a, int mode, const Core& c, const Geo& g, const KArgs& a, const FourStep& fs,
                         unsigned blocks, long long elems, cudaStream_t s, bool library_only, int jit_opt, int tc) {
+  // Plan-time kernels carry the L2-priority choice in the mode's bit 2.
+  const int jmode = mode | (fs.l2_hints ? 4 : 0);
   if (tc > 0 && !library_only) {
-    const int r = jit_launch_tc(pass_a ? Kernel::COLS_TW : Kernel::ROWS_T, c, tc, g.tpb, a, blocks, s, mode, &fs);
+    const int r = jit_launch_tc(pass_a ? Kernel::COLS_TW : Kernel::ROWS_T, c, tc, g.tpb, a, blocks, s, jmode, &fs);
     if (r == 2) throw Fail{CHFFT_ECUDA, "launch of a tensor-core kernel failed"};
     if (r == 1) throw Fail{CHFFT_EUNSUPPORTED, "tensor-core kernel unavailable (plan compiler or geometry)"};
     return;
   }
   if (!library_only && want_specialised(elems, jit_opt) &&
-      jit_launch(pass_a ? Kernel::COLS_TW : Kernel::ROWS_T, c.dtype, c, g, a, blocks, s, mode, &fs) == 0)
+      jit_launch(pass_a ? Kernel::COLS_TW : Kernel::ROWS_T, c.dtype, c, g, a, blocks, s, jmode, &fs) == 0)
     return;
   CHFFT_CUDA(c.dtype == 0 ? launch_fourstep<float>(pass_a, mode, g.k1, a, fs, blocks, g.threads, g.smem, s)
                           : launch_fourstep<double>(pass_a, mode, g.k1, a, fs, blocks, g.threads, g.smem, s));
@@ -477,13 +481,17 @@ FourStep BigCore::fs() const {
   f.lo = lo.p;
   f.hi = hi.p;
   f.n_user = n;
+  f.l2_hints = opts.l2_hints > 0 ? 1 : 0;
   f.chirp = chirp.p;
   f.bhat = bhat.p;
   return f;
 }
 
 long long BigCore::chunk(long long batch) const {
-  long long budget_mb = opts.l2_mb > 0 ? opts.l2_mb : 64;
+  // Chunks bound the workspace; within one GB300 the intermediate goes back
+  // to HBM whatever the chunk (measured), so few large chunks (few launches,
+  // full waves) are fastest.
+  long long budget_mb = opts.l2_mb > 0 ? opts.l2_mb : 512;
   if (const char* e = std::getenv("CHFFT_L2_BUDGET_MB")) budget_mb = std::max(1LL, std::atoll(e));
   const long long per = m * (long long)cplx_bytes(dtype) * (blue ? 2 : 1);
   return std::max(1LL, std::min(batch, (budget_mb << 20) / per));
@@ -498,7 +506,9 @@ void BigCore::exec(const void* in, void* out, void* work, long long batch, bool 
   char* tmp = static_cast<char*>(work);
   char* tmp2 = tmp + g * m * cb_;
   const FourStep f = fs();
-  Geo ga = col_geo(ca, n2, opts.fs_tpb, opts), gb = col_geo(cb, n1, opts.fs_tpb, opts);
+  // f32 tiles of 8 columns / rows: two CTAs per SM (measured faster than 16).
+  const int tile_default = opts.fs_tpb > 0 ? opts.fs_tpb : (dtype == 0 ? 8 : 0);
+  Geo ga = col_geo(ca, n2, tile_default, opts), gb = col_geo(cb, n1, tile_default, opts);
   const int tc = library_only ? 0 : opts.tc;
   if (tc > 0) {
     // Tile widths the tensor-core kernels take (largest first, from the knob).

@@ -30,6 +30,8 @@ PlanOpts to_opts(const chfft_plan_config& c) {
   o.tc = c.tc_precision;
   o.min_blocks = c.min_blocks_per_sm;
   o.balance = c.balanced;
+  o.prefetch = c.l2_prefetch;
+  o.l2_hints = c.l2_evict_hints;
   return o;
 }
 
@@ -46,6 +48,8 @@ chfft_plan_config to_cfg(const PlanOpts& o) {
   c.tc_precision = o.tc;
   c.min_blocks_per_sm = o.min_blocks;
   c.balanced = o.balance;
+  c.l2_prefetch = o.prefetch;
+  c.l2_evict_hints = o.l2_hints;
   return c;
 }
 
@@ -78,9 +82,10 @@ struct Resolved {
   int npass = 0, rfirst = 0, rlast = 0;
   int minb = 0;          // specialised kernels: launch-bounds CTAs per SM
   bool balanced = false;  // specialised kernels: balanced mixed-radix variant
+  int prefetch = 0;       // specialised kernels: next-wave L2 prefetch knob (-1 auto, 0 off, 1 on)
 
   auto key() const {
-    return std::make_tuple(big, blue, k1, jit, wide, tpb, tile, n1, fft_len, l2mb, chunks, minb, balanced);
+    return std::make_tuple(big, blue, k1, jit, wide, tpb, tile, n1, fft_len, l2mb, chunks, minb, balanced, prefetch);
   }
 };
 
@@ -158,19 +163,20 @@ Resolved resolve(const PlanImpl& p, long long batch, const PlanOpts& o) {
         make_stages(r.n1, &sa);
         make_stages(r.n2, &sb);
         const Core ca = shell(sa, dt);
-        const Geo ga = col_geo(ca, r.n2, o.fs_tpb, o);
+        const int tile_default = o.fs_tpb > 0 ? o.fs_tpb : (dt == 0 ? 8 : 0);
+        const Geo ga = col_geo(ca, r.n2, tile_default, o);
         r.jit = jit_on() && want_specialised(batch * m, o.jit);
         bool wide = false;
         const StageList ea = effective(sa, dt, ga, r.jit, &wide);
         bool wide_b = false;
-        const StageList eb = effective(sb, dt, col_geo(shell(sb, dt), r.n1, o.fs_tpb, o), r.jit, &wide_b);
+        const StageList eb = effective(sb, dt, col_geo(shell(sb, dt), r.n1, tile_default, o), r.jit, &wide_b);
         r.wide = wide || wide_b;
         r.k1 = ga.k1;
         r.tpb = ga.tpb;
         r.tile = ga.tpb;
         r.threads = ga.threads;
         r.smem = ga.smem;
-        r.l2mb = o.l2_mb > 0 ? o.l2_mb : 64;
+        r.l2mb = o.l2_mb > 0 ? o.l2_mb : 512;
         const long long per = m * (long long)cplx_bytes(dt) * (r.blue ? 2 : 1);
         const long long chunk = std::max(1LL, std::min(batch, (r.l2mb << 20) / per));
         r.chunks = (batch + chunk - 1) / chunk;
@@ -207,6 +213,7 @@ Resolved resolve(const PlanImpl& p, long long batch, const PlanOpts& o) {
       one_cta(p.core.st, batch);
       break;
   }
+  r.prefetch = r.jit ? o.prefetch : 0;
   return r;
 }
 
@@ -280,6 +287,7 @@ void features(const PlanImpl& p, long long batch, const PlanOpts& o, float* f) {
   f[k++] = (float)lg2((double)len * (double)batch);
   f[k++] = (float)lg2((double)r.chunks);
   f[k++] = (float)r.minb;
+  f[k++] = (float)r.prefetch;
 }
 
 // Bluestein lengths to try: the cheapest M by the engine's cost rule and the
@@ -325,6 +333,9 @@ std::vector<PlanOpts> candidates(const PlanImpl& p, long long batch, bool tune_j
           q = o;
           q.balance = 0;
           out.push_back(q);
+          q = o;
+          q.prefetch = 1;
+          out.push_back(q);
         }
       }
     }
@@ -356,7 +367,7 @@ std::vector<PlanOpts> candidates(const PlanImpl& p, long long batch, bool tune_j
           std::sort(sp.begin(), sp.end());
           for (size_t i = 0; i < sp.size() && i < 3; i++)
             for (int tile : dt == 0 ? std::vector<int>{8, 16} : std::vector<int>{4, 8})
-              for (int l2 : {32, 96}) {
+              for (int l2 : {64, 512}) {
                 PlanOpts o = base;
                 o.fs_n1 = sp[i].second;
                 o.fs_tpb = tile;

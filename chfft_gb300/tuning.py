@@ -19,7 +19,7 @@ import numpy as np
 
 from . import METHODS, _check, lib
 
-FEATURES = 40
+FEATURES = 48
 
 
 class PlanConfig(ctypes.Structure):
@@ -27,7 +27,8 @@ class PlanConfig(ctypes.Structure):
         ("k1", ctypes.c_int), ("seq_per_cta", ctypes.c_int), ("max_radix", ctypes.c_int), ("jit", ctypes.c_int),
         ("bluestein_len", ctypes.c_longlong), ("fs_n1", ctypes.c_int), ("tile_cols", ctypes.c_int),
         ("l2_chunk_mb", ctypes.c_int), ("tc_precision", ctypes.c_int), ("min_blocks_per_sm", ctypes.c_int),
-        ("balanced", ctypes.c_int),
+        ("balanced", ctypes.c_int), ("l2_prefetch", ctypes.c_int),
+        ("l2_evict_hints", ctypes.c_int),
     ]
 
     def as_dict(self):

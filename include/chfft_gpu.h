@@ -235,7 +235,7 @@ typedef struct chfft_plan_config {
   long long bluestein_len; /* Bluestein convolution length M (7-smooth, >= 2N-1), 0 auto */
   int fs_n1;               /* four-step column length n1 (n1 | N), 0 auto */
   int tile_cols;           /* four-step and 2-D column tile width, 0 auto */
-  int l2_chunk_mb;         /* four-step chunk budget in MiB, 0 auto (64) */
+  int l2_chunk_mb;         /* four-step chunk budget in MiB (the workspace), 0 auto (512) */
   int tc_precision;        /* f32 radix-16 passes on the tensor cores (power-of-two CFft1D
                               lengths >= 16, plan-time compiled): 0 off (FP32 cores),
                               1 FP16 hi+lo, 2 BF16 hi+lo, 3 BF16 hi+mid+lo; FP32 accumulation */
@@ -244,6 +244,13 @@ typedef struct chfft_plan_config {
   int balanced;            /* plan-time kernels with mixed radices: 1 / -1 (auto) every thread
                               takes maxR / R butterflies of a radix-R pass, 0 one butterfly per
                               thread and pass (threads idle through the larger radices) */
+  int l2_prefetch;         /* plan-time row / column / four-step kernels: 1 every CTA asks L2 for
+                              the input of the CTA one wave later (the next wave's HBM reads
+                              overlap this wave's passes), 0 / -1 (auto) off: measured slower on
+                              the configurations timed so far, kept as a tuning knob */
+  int l2_evict_hints;      /* four-step passes: 1 the intermediate is stored with an L2
+                              evict_last policy and the streamed input / output with
+                              evict_first; 0 / -1 (auto) plain accesses */
 } chfft_plan_config;
 
 CHFFT_API void chfft_plan_config_default(chfft_plan_config* cfg);
@@ -257,7 +264,7 @@ CHFFT_API int chfft_plan_get_config(chfft_plan plan, chfft_plan_config* cfg);
 CHFFT_API int chfft_plan_candidates(chfft_plan plan, size_t batch, int tune_jit, chfft_plan_config* out, int cap,
                                     int* n);
 /* Cost-model features of (plan, batch, cfg): CHFFT_FEATURES floats. */
-#define CHFFT_FEATURES 40
+#define CHFFT_FEATURES 48
 CHFFT_API int chfft_plan_features(chfft_plan plan, size_t batch, const chfft_plan_config* cfg, float* out);
 /* Exhaustive autotune: times every candidate (the method on `batch`
  * transforms of device scratch data, median of `reps` launches after one

@@ -5,7 +5,7 @@ import pytest
 
 from oracle import mlp as omlp
 
-F = 40
+F = 48
 
 
 @pytest.mark.parametrize("h,n", [(8, 5), (16, 40), (64, 12)])
