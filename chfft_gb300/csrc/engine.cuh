@@ -315,6 +315,7 @@ template <bool BLUE, bool TMINOR, bool FUSED, bool K1>
 struct DynCore {
   static constexpr bool kK1 = K1;
   static constexpr bool kStatic = false;
+  static constexpr int kThreads = kMaxThreads;
   static constexpr int kMinBlocks = K1 ? 2 : 1;  // launch bounds: resident CTAs per SM
   // The kernel's shared-memory tile (layout shared with the kernel's own
   // pre-/post-phases).
@@ -362,13 +363,16 @@ struct SpectrumStore {
   }
 };
 
-// MINB: the resident CTAs per SM the kernel's launch bounds ask for (the
-// register budget follows from it); EPT: elements per thread of the
-// several-butterflies variant (0: the dtype's default).
-template <bool BLUE, bool TMINOR, bool K1, int M, int NU, int TPB, int LD, int P, int MINB, int EPT, int... Rs>
+// THR: the threads the kernel is launched with; MINB: the resident CTAs per
+// SM its launch bounds ask for (the register budget follows from both);
+// EPT: elements per thread of the several-butterflies variant (0: the
+// dtype's default).
+template <bool BLUE, bool TMINOR, bool K1, int M, int NU, int TPB, int LD, int P, int THR, int MINB, int EPT,
+          int... Rs>
 struct StatCore {
   static constexpr bool kK1 = K1;
   static constexpr bool kStatic = true;
+  static constexpr int kThreads = THR;
   static constexpr int kMinBlocks = MINB;
   template <typename C>
   __device__ __forceinline__ static SmemIO<C, P> tile(unsigned char* base, int) {

@@ -157,9 +157,13 @@ std::string name_expression(Kernel k, int dtype, const Core& c, const StageList&
   s += c.blue ? "true," : "false,";
   s += column_mapped(k) ? "true," : "false,";
   s += g.k1 ? "true," : "false,";
-  const int minb = g.min_blocks > 0 ? g.min_blocks : (g.k1 || g.ept > 0 ? 2 : 1);
+  // Default register budget: that of 512-thread CTAs, 2 per SM for the
+  // one-butterfly and balanced variants, 1 otherwise.
+  const int minb = g.min_blocks > 0 ? g.min_blocks
+                                    : std::max(1, (g.k1 || g.ept > 0 ? 2 : 1) * (kMaxThreads / std::max(32, g.threads)));
   s += std::to_string(sl.n) + "," + std::to_string(c.n) + "," + std::to_string(g.tpb) + "," + std::to_string(g.ld) +
-       "," + std::to_string(pad_period(sl)) + "," + std::to_string(minb) + "," + std::to_string(g.k1 ? 0 : g.ept);
+       "," + std::to_string(pad_period(sl)) + "," + std::to_string(g.threads) + "," + std::to_string(minb) + "," +
+       std::to_string(g.k1 ? 0 : g.ept);
   for (int r : pass_order(sl)) s += "," + std::to_string(r);
   s += ">";
   if (four_step(k)) s += ", " + std::to_string(mode);

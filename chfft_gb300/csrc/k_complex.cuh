@@ -59,7 +59,7 @@ struct RowStore {
 };
 
 template <typename T, class CoreT>
-__global__ void __launch_bounds__(kMaxThreads, CoreT::kMinBlocks) k_c2c(const KArgs a) {
+__global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_c2c(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
@@ -104,7 +104,7 @@ struct ColStore {
 };
 
 template <typename T, class CoreT>
-__global__ void __launch_bounds__(kMaxThreads, CoreT::kMinBlocks) k_cols(const KArgs a) {
+__global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_cols(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
@@ -186,7 +186,7 @@ struct ColsAStore {
 };
 
 template <typename T, class CoreT, int MODE>
-__global__ void __launch_bounds__(kMaxThreads, CoreT::kMinBlocks) k_cols_tw(const KArgs a, const FourStep fs) {
+__global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_cols_tw(const KArgs a, const FourStep fs) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
@@ -262,7 +262,7 @@ struct RowsBLoad {
 };
 
 template <typename T, class CoreT, int MODE>
-__global__ void __launch_bounds__(kMaxThreads, CoreT::kMinBlocks) k_rows_t(const KArgs a, const FourStep fs) {
+__global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_rows_t(const KArgs a, const FourStep fs) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const auto sm = CoreT::template tile<C>(smem_raw, a.ld);

@@ -43,7 +43,7 @@ struct PackLoad {
 };
 
 template <typename T, class CoreT>
-__global__ void __launch_bounds__(kMaxThreads, CoreT::kMinBlocks) k_r2c(const KArgs a) {
+__global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_r2c(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
@@ -89,7 +89,7 @@ struct UnpackStore {
 };
 
 template <typename T, class CoreT>
-__global__ void __launch_bounds__(kMaxThreads, CoreT::kMinBlocks) k_c2r(const KArgs a) {
+__global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_c2r(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
@@ -141,7 +141,7 @@ struct DctPackLoad {
 };
 
 template <typename T, class CoreT>
-__global__ void __launch_bounds__(kMaxThreads, CoreT::kMinBlocks) k_dct2(const KArgs a) {
+__global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_dct2(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
@@ -209,7 +209,7 @@ struct DctUnpackStore {
 };
 
 template <typename T, class CoreT>
-__global__ void __launch_bounds__(kMaxThreads, CoreT::kMinBlocks) k_dct3(const KArgs a) {
+__global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_dct3(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
@@ -298,7 +298,7 @@ struct MdctStore {
 };
 
 template <typename T, class CoreT>
-__global__ void __launch_bounds__(kMaxThreads, CoreT::kMinBlocks) k_mdct(const KArgs a) {
+__global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_mdct(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
@@ -356,7 +356,7 @@ struct ImdctStore {
 };
 
 template <typename T, class CoreT>
-__global__ void __launch_bounds__(kMaxThreads, CoreT::kMinBlocks) k_imdct(const KArgs a) {
+__global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_imdct(const KArgs a) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const auto sm = CoreT::template tile<C>(smem_raw, a.ld);

@@ -98,6 +98,7 @@ template <bool TMINOR, int N, int TPB, int LD, int PREC, int R0, int S16>
 struct TcCore {
   static constexpr bool kK1 = false;
   static constexpr bool kStatic = true;
+  static constexpr int kThreads = kTcThreads;
   static constexpr int kMinBlocks = 1;
   static constexpr int P = 16;                       // tile pad period
   static constexpr int NP = PREC == 3 ? 3 : 2;       // 16-bit parts per operand
