@@ -137,6 +137,12 @@ __global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_cols(con
 // bit 2 (kL2Hints) L2 eviction priorities: the intermediate is stored
 // evict_last so pass B can find it in L2, streamed data goes evict_first.
 constexpr int kL2Hints = 4;
+// Bit 3 (kSmemTwiddle): pass A builds, per CTA, the tables
+// A[t][q] = w_N^(32 q c) and B[t][r] = w_N^(r c) (c = c0 + t, q < ceil(N1 / 32),
+// r < 32) in shared memory after its tile, so the store's w_N^(k1 c) =
+// A[t][k1 / 32] B[t][k1 % 32] costs two shared loads instead of two global
+// table loads per element.
+constexpr int kSmemTwiddle = 8;
 
 // Pass A loader: MODE 0 plain (scale, conjugate for backward); MODE 1 the
 // Bluestein input x_j c_j for flat index j = n1 N2 + n2 < n_user, else 0.
@@ -166,18 +172,25 @@ struct ColsALoad {
   }
 };
 
-template <typename C, bool HINTS>
+template <typename C, bool HINTS, bool STWID = false>
 struct ColsAStore {
   C* out;
   int ncols, nvalid, c0;
   const FourStep* fs;
   unsigned long long pol;  // L2 policy of the intermediate (HINTS)
+  const C* tw;             // STWID: the per-CTA tables A (tpb x qa) then B (tpb x 33), rows padded
+  int qa, tpb;
   __device__ __forceinline__ void store(int t, int k1, C v) const {
     if (t >= nvalid) return;
-    const long long e = (long long)k1 * (c0 + t);  // < N
-    const C* lo = static_cast<const C*>(fs->lo);
-    const C* hi = static_cast<const C*>(fs->hi);
-    const C w = cmul(__ldg(&hi[e >> fs->tw_shift]), __ldg(&lo[e & ((1LL << fs->tw_shift) - 1)]));
+    C w;
+    if constexpr (STWID) {
+      w = cmul(tw[t * qa + (k1 >> 5)], tw[tpb * qa + t * 33 + (k1 & 31)]);
+    } else {
+      const long long e = (long long)k1 * (c0 + t);  // < N
+      const C* lo = static_cast<const C*>(fs->lo);
+      const C* hi = static_cast<const C*>(fs->hi);
+      w = cmul(__ldg(&hi[e >> fs->tw_shift]), __ldg(&lo[e & ((1LL << fs->tw_shift) - 1)]));
+    }
     if constexpr (HINTS)
       st_policy(out + (long long)k1 * ncols + t, cmul(v, w), pol);
     else
@@ -211,7 +224,25 @@ __global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_cols_tw(
   const unsigned long long pout = kHints ? l2_evict_last() : 0ull;
   ColsALoad<C, MODE & 3, kHints> ld{(const C*)a.in + tr * a.in_dist + c0, a.ncols, nvalid, c0, (T)a.scale, a.back,
                                     &fs, pin};
-  ColsAStore<C, kHints> st{(C*)a.out + tr * a.out_dist + c0, a.ncols, nvalid, c0, &fs, pout};
+  constexpr bool kStw = (MODE & kSmemTwiddle) != 0;
+  C* twt = nullptr;
+  const int qa = smem_twiddle_stride_a(fs.n1);
+  if constexpr (kStw) {
+    // Tables after the tile (16-byte aligned); the core's first barrier
+    // orders these writes before the last pass reads them.
+    twt = reinterpret_cast<C*>(smem_raw + (((size_t)a.tpb * a.ld * sizeof(C) + 15) / 16) * 16);
+    const C* lo = static_cast<const C*>(fs.lo);
+    const C* hi = static_cast<const C*>(fs.hi);
+    const long long mask = (1LL << fs.tw_shift) - 1;
+    for (int i = threadIdx.x; i < a.tpb * (qa + 33); i += blockDim.x) {
+      const bool in_a = i < a.tpb * qa;
+      const int t = in_a ? i / qa : (i - a.tpb * qa) / 33;
+      const int q = in_a ? i - t * qa : (i - a.tpb * qa) - t * 33;
+      const long long e = ((long long)(in_a ? 32 * q : q) * (c0 + t)) % fs.n;  // w_N^N = 1
+      twt[i] = cmul(__ldg(&hi[e >> fs.tw_shift]), __ldg(&lo[e & mask]));
+    }
+  }
+  ColsAStore<C, kHints, kStw> st{(C*)a.out + tr * a.out_dist + c0, a.ncols, nvalid, c0, &fs, pout, twt, qa, a.tpb};
   CoreT::run(a.core, a.tpb, sm, ld, st);
 }
 

@@ -59,6 +59,14 @@ struct FourStep {
   int l2_hints;       // host side: the plan-time kernels run with L2 eviction priorities (mode bit 2)
 };
 
+// Pass A's per-CTA twiddle tables: tpb rows of ceil(n1 / 32) entries, then
+// tpb rows of 32, both rows padded to an odd stride (no bank conflicts when
+// the lanes of a warp read adjacent columns).
+__host__ __device__ constexpr int smem_twiddle_stride_a(int n1) { return ((n1 + 31) / 32) | 1; }
+__host__ __device__ constexpr int smem_twiddle_entries(int tpb, int n1) {
+  return tpb * (smem_twiddle_stride_a(n1) + 33);
+}
+
 // Global accesses with an L2 eviction-priority policy (createpolicy).
 __device__ __forceinline__ unsigned long long l2_evict_first() {
   unsigned long long p;

@@ -384,7 +384,7 @@ bool four_step_split(long long m, int dtype, int* n1, int* n2) {
 static void launch_pass(bool pass_a, int mode, const Core& c, const Geo& g, const KArgs& a, const FourStep& fs,
                         unsigned blocks, long long elems, cudaStream_t s, bool library_only, int jit_opt, int tc) {
   // Plan-time kernels carry the L2-priority choice in the mode's bit 2.
-  const int jmode = mode | (fs.l2_hints ? 4 : 0);
+  const int jmode = mode | (fs.l2_hints ? 4 : 0) | (pass_a && tc <= 0 ? 8 : 0);
   if (tc > 0 && !library_only) {
     const int r = jit_launch_tc(pass_a ? Kernel::COLS_TW : Kernel::ROWS_T, c, tc, g.tpb, a, blocks, s, jmode, &fs);
     if (r == 2) throw Fail{CHFFT_ECUDA, "launch of a tensor-core kernel failed"};
