@@ -99,7 +99,7 @@ struct TcCore {
   static constexpr bool kK1 = false;
   static constexpr bool kStatic = true;
   static constexpr int kThreads = kTcThreads;
-  static constexpr int kMinBlocks = 1;
+  static constexpr int kMinBlocks = 3;
   static constexpr int P = 16;                       // tile pad period
   static constexpr int NP = PREC == 3 ? 3 : 2;       // 16-bit parts per operand
   static constexpr int ROWS = TPB * (N / 16);        // butterflies per radix-16 pass
