@@ -341,8 +341,9 @@ def run_gpu(args, rank, world, local_rank):
 
 
 # ---------------------------------------------------------------------------- other configurations
-# Optional workloads (--workload): the other BASELINE configurations, measured
-# the same way; the default workload above is the headline line.
+# Optional workloads (--workload): the other benchmark configurations (large
+# batches, uneven batches, the learned cost model, f64 latency), measured the
+# same way; the default workload above is the headline line.
 
 def smooth_numbers(lo, hi, primes=(2, 3, 5)):
     out = {1}
