@@ -789,7 +789,7 @@ def run_costmodel(args):
         "data": "synthetic (device scratch bytes 0x3c); lengths log-uniform in [64, 2^22], seeded",
         "config": {"workload": f"learned plan cost model: {len(train_len)} training lengths x batch {{1, 64, 4096}} "
                                f"(<= 2^24 elements), {len(test_len)} held-out lengths; CFft1D f32 forward",
-                   "model": "MLP 40-64-64-1 ReLU FP32, Adam, 200 epochs, trained by the library's CUDA kernels",
+                   "model": f"MLP {tuning.FEATURES}-64-64-1 ReLU FP32, Adam, 200 epochs, trained by the library's CUDA kernels",
                    "timing": "median of 3 CUDA-event launches after 1 warm-up, per candidate",
                    "kernels": "library kernels (plan-time compilation off)"},
         "held_out": {

@@ -121,6 +121,10 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_batch(const BatchArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* sbase = reinterpret_cast<C*>(smem_raw);
   __shared__ int s_task;
+  // The task's item descriptor, copied once per task: its fields are read
+  // all through the task, from shared memory instead of global memory.
+  __shared__ __align__(16) BatchItem s_item;
+  static_assert(sizeof(BatchItem) % 4 == 0, "item descriptor copied as 32-bit words");
   for (;;) {
     __syncthreads();
     if (threadIdx.x == 0) s_task = atomicAdd(A.next, 1);
@@ -128,8 +132,14 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_batch(const BatchArgs A) {
     const int ti = s_task;
     if (ti >= A.ntasks) return;
     const BatchTask tk = A.tasks[ti];
-    if (tk.wait_ctr >= 0) wait_for(A, tk.wait_ctr, tk.wait_target);
-    const BatchItem& it = A.items[tk.item];
+    {
+      const int* src = reinterpret_cast<const int*>(A.items + tk.item);
+      int* dst = reinterpret_cast<int*>(&s_item);
+      for (int w = threadIdx.x; w < (int)(sizeof(BatchItem) / 4); w += blockDim.x) dst[w] = __ldg(src + w);
+    }
+    if (tk.wait_ctr >= 0) wait_for(A, tk.wait_ctr, tk.wait_target);  // ends with a barrier
+    else __syncthreads();
+    const BatchItem& it = s_item;
     const int tid = threadIdx.x, nth = blockDim.x;
 
     if (tk.type == BT_POST) {

@@ -178,13 +178,13 @@ struct ColsAStore {
   int ncols, nvalid, c0;
   const FourStep* fs;
   unsigned long long pol;  // L2 policy of the intermediate (HINTS)
-  const C* tw;             // STWID: the per-CTA tables A (tpb x qa) then B (tpb x 33), rows padded
-  int qa, tpb;
+  const C* tw;             // STWID: the per-CTA tables A (tpb x qa) then B (tpb x qb), rows padded
+  int qa, qb, tpb;
   __device__ __forceinline__ void store(int t, int k1, C v) const {
     if (t >= nvalid) return;
     C w;
     if constexpr (STWID) {
-      w = cmul(tw[t * qa + (k1 >> 5)], tw[tpb * qa + t * 33 + (k1 & 31)]);
+      w = cmul(tw[t * qa + (k1 >> 5)], tw[tpb * qa + t * qb + (k1 & 31)]);
     } else {
       const long long e = (long long)k1 * (c0 + t);  // < N
       const C* lo = static_cast<const C*>(fs->lo);
@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_cols_tw(
                                     &fs, pin};
   constexpr bool kStw = (MODE & kSmemTwiddle) != 0;
   C* twt = nullptr;
-  const int qa = smem_twiddle_stride_a(fs.n1);
+  const int qa = smem_twiddle_stride_a(fs.n1), qb = smem_twiddle_stride_b(a.tpb);
   if constexpr (kStw) {
     // Tables after the tile (16-byte aligned); the core's first barrier
     // orders these writes before the last pass reads them.
@@ -234,15 +234,16 @@ __global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_cols_tw(
     const C* lo = static_cast<const C*>(fs.lo);
     const C* hi = static_cast<const C*>(fs.hi);
     const long long mask = (1LL << fs.tw_shift) - 1;
-    for (int i = threadIdx.x; i < a.tpb * (qa + 33); i += blockDim.x) {
+    for (int i = threadIdx.x; i < a.tpb * (qa + qb); i += blockDim.x) {
       const bool in_a = i < a.tpb * qa;
-      const int t = in_a ? i / qa : (i - a.tpb * qa) / 33;
-      const int q = in_a ? i - t * qa : (i - a.tpb * qa) - t * 33;
+      const int t = in_a ? i / qa : (i - a.tpb * qa) / qb;
+      const int q = in_a ? i - t * qa : (i - a.tpb * qa) - t * qb;
       const long long e = ((long long)(in_a ? 32 * q : q) * (c0 + t)) % fs.n;  // w_N^N = 1
       twt[i] = cmul(__ldg(&hi[e >> fs.tw_shift]), __ldg(&lo[e & mask]));
     }
   }
-  ColsAStore<C, kHints, kStw> st{(C*)a.out + tr * a.out_dist + c0, a.ncols, nvalid, c0, &fs, pout, twt, qa, a.tpb};
+  ColsAStore<C, kHints, kStw> st{(C*)a.out + tr * a.out_dist + c0, a.ncols, nvalid, c0, &fs, pout, twt, qa, qb,
+                                 a.tpb};
   CoreT::run(a.core, a.tpb, sm, ld, st);
 }
 

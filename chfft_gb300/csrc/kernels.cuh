@@ -60,11 +60,14 @@ struct FourStep {
 };
 
 // Pass A's per-CTA twiddle tables: tpb rows of ceil(n1 / 32) entries, then
-// tpb rows of 32, both rows padded to an odd stride (no bank conflicts when
-// the lanes of a warp read adjacent columns).
+// tpb rows of 32. The lanes of a warp read column t = lane % tpb, row
+// offset j = lane / tpb: table A at one row offset for all lanes (an odd
+// stride spreads the tpb rows over the banks), table B at t * S + j, which
+// is conflict-free for S = 32 + 32 / tpb.
 __host__ __device__ constexpr int smem_twiddle_stride_a(int n1) { return ((n1 + 31) / 32) | 1; }
+__host__ __device__ constexpr int smem_twiddle_stride_b(int tpb) { return 32 + (tpb < 32 ? 32 / tpb : 1); }
 __host__ __device__ constexpr int smem_twiddle_entries(int tpb, int n1) {
-  return tpb * (smem_twiddle_stride_a(n1) + 33);
+  return tpb * (smem_twiddle_stride_a(n1) + smem_twiddle_stride_b(tpb));
 }
 
 // Global accesses with an L2 eviction-priority policy (createpolicy).
