@@ -339,7 +339,10 @@ Geo col_geo(const Core& c, int ncols, int tpb_opt, const PlanOpts& o) {
   g.min_blocks = o.min_blocks;
   g.balance = o.balance;
   g.prefetch = o.prefetch;
-  const int ept = ept_of(c.dtype);
+  // Elements per thread of the several-butterflies variant: the dtype's
+  // default, or the `ept` knob (specialised kernels; a library kernel keeps
+  // its own and leaves the extra threads idle).
+  const int ept = o.ept > 0 ? o.ept : ept_of(c.dtype);
   g.ld = smem_ld(c.st.n);
   const size_t per = (size_t)g.ld * cplx_bytes(c.dtype);
   int tpb = tpb_opt > 0 ? tpb_opt : (c.dtype == 0 ? 16 : 8);  // 128-byte row segments
@@ -347,6 +350,7 @@ Geo col_geo(const Core& c, int ncols, int tpb_opt, const PlanOpts& o) {
   while (tpb > 1 && ((size_t)tpb * per > kMaxSmem || threads_needed(c.st, ept, tpb) > kMaxThreads)) tpb--;
   g.tpb = tpb;
   g.k1 = o.k1 != 0 && threads_needed(c.st, ept, tpb, true) <= kMaxThreads;
+  if (!g.k1 && o.ept > 0) g.ept = o.ept;
   int th = threads_needed(c.st, ept, tpb, g.k1);
   th = std::max(32, ((th + 31) / 32) * 32);
   g.threads = std::min(th, kMaxThreads);

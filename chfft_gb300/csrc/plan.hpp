@@ -85,6 +85,7 @@ struct PlanOpts {
   int tc = 0;            // f32 radix-16 passes on tensor cores: 0 off, 1 FP16x2, 2 BF16x2, 3 BF16x3
   int min_blocks = 0;    // specialised kernels: launch-bounds CTAs per SM, 0 auto
   int balance = -1;      // specialised kernels: balanced mixed-radix variant (-1 auto = on, 0 off, 1 on)
+  int ept = 0;           // column kernels: elements per thread of the several-butterflies variant, 0 default
   int prefetch = -1;     // specialised row / column kernels: L2 prefetch of the next wave (1 on; -1 auto = off, 0 off)
   int l2_hints = -1;     // four-step passes: L2 eviction priorities (intermediate kept, streams first) (1 on; -1 auto = off)
 };

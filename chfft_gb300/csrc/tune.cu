@@ -32,6 +32,7 @@ PlanOpts to_opts(const chfft_plan_config& c) {
   o.balance = c.balanced;
   o.prefetch = c.l2_prefetch;
   o.l2_hints = c.l2_evict_hints;
+  o.ept = c.col_elems_per_thread;
   return o;
 }
 
@@ -50,6 +51,7 @@ chfft_plan_config to_cfg(const PlanOpts& o) {
   c.balanced = o.balance;
   c.l2_prefetch = o.prefetch;
   c.l2_evict_hints = o.l2_hints;
+  c.col_elems_per_thread = o.ept;
   return c;
 }
 

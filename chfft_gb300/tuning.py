@@ -28,7 +28,7 @@ class PlanConfig(ctypes.Structure):
         ("bluestein_len", ctypes.c_longlong), ("fs_n1", ctypes.c_int), ("tile_cols", ctypes.c_int),
         ("l2_chunk_mb", ctypes.c_int), ("tc_precision", ctypes.c_int), ("min_blocks_per_sm", ctypes.c_int),
         ("balanced", ctypes.c_int), ("l2_prefetch", ctypes.c_int),
-        ("l2_evict_hints", ctypes.c_int),
+        ("l2_evict_hints", ctypes.c_int), ("col_elems_per_thread", ctypes.c_int),
     ]
 
     def as_dict(self):

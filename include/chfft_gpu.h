@@ -251,6 +251,9 @@ typedef struct chfft_plan_config {
   int l2_evict_hints;      /* four-step passes: 1 the intermediate is stored with an L2
                               evict_last policy and the streamed input / output with
                               evict_first; 0 / -1 (auto) plain accesses */
+  int col_elems_per_thread; /* column / four-step kernels of the several-butterflies variant:
+                               complex elements a thread holds (16 or 32), 0 the dtype's
+                               default (32 f32, 16 f64) */
 } chfft_plan_config;
 
 CHFFT_API void chfft_plan_config_default(chfft_plan_config* cfg);
