@@ -311,10 +311,12 @@ Geo row_geo(const Core& c, long long count, const PlanOpts& o) {
   const int t1k = std::max(1, threads_needed(c.st, ept, 1, true));
   const bool k1 = t1k <= kMaxThreads && o.k1 != 0;
   if (k1) {
-    // One butterfly per thread: fill the CTA up to 512 threads, keeping two
-    // CTAs' tiles within an SM's shared memory.
+    // One butterfly per thread: sequences up to about 256 threads per CTA
+    // (the autotuner's pick on GB300: N=1000 2 sequences, 26.6 -> 19.8 us;
+    // N=4096 1 sequence, 213 -> 189 us for 16384), keeping two CTAs' tiles
+    // within an SM's shared memory.
     g.k1 = true;
-    int tpb = o.tpb > 0 ? std::min(o.tpb, kMaxThreads / t1k) : std::max(1, kMaxThreads / t1k);
+    int tpb = o.tpb > 0 ? std::min(o.tpb, kMaxThreads / t1k) : std::max(1, 256 / t1k);
     tpb = (int)std::min<size_t>(tpb, std::max<size_t>(1, (o.tpb > 0 ? kMaxSmem : kMaxSmem / 2) / per));
     tpb = (int)std::max<long long>(1, std::min<long long>(tpb, count));
     g.tpb = tpb;

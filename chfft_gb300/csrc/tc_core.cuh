@@ -99,7 +99,6 @@ struct TcCore {
   static constexpr bool kK1 = false;
   static constexpr bool kStatic = true;
   static constexpr int kThreads = kTcThreads;
-  static constexpr int kMinBlocks = 3;
   static constexpr int P = 16;                       // tile pad period
   static constexpr int NP = PREC == 3 ? 3 : 2;       // 16-bit parts per operand
   static constexpr int ROWS = TPB * (N / 16);        // butterflies per radix-16 pass
@@ -112,6 +111,9 @@ struct TcCore {
   static constexpr int B_BYTES = NP * 32 * 64;
   static constexpr int BAR_OFF = B_OFF + B_BYTES;
   static constexpr int SMEM = BAR_OFF + 16;
+  // Launch bounds: as many resident CTAs as the shared memory allows, up to
+  // three (79 registers at three: no spills).
+  static constexpr int kMinBlocks = 3 * SMEM <= 227 * 1024 ? 3 : 2 * SMEM <= 227 * 1024 ? 2 : 1;
   static constexpr int TMEM_COLS = (32 * T <= 32) ? 32 : (32 * T <= 64) ? 64 : (32 * T <= 128) ? 128 : (32 * T <= 256) ? 256 : 512;
   static_assert(N == R0 * (S16 == 1 ? 16 : S16 == 2 ? 256 : S16 == 3 ? 4096 : 65536), "N = R0 * 16^S16");
   static_assert(ROWS % 128 == 0 && T >= 1 && T <= 16, "radix-16 rows must fill M = 128 tiles");
