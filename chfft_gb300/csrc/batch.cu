@@ -37,6 +37,15 @@ bool batch_fits(const StageList& st, int tpb) {
   return threads_needed(st, kBatchEpt, tpb) <= kBatchThreads && (size_t)tpb * smem_ld(st.n) * 8 <= kBatchSmemCap;
 }
 
+// Four-step tile width of a core: the widest power of two from kBatchTile
+// to kBatchTileMax whose tile fits one CTA. Wider tiles mean fewer tasks, so
+// less per-task overhead (ticket, descriptor, waits, signal) per element.
+int fs_width(const StageList& st) {
+  int w = kBatchTile;
+  while (w * 2 <= kBatchTileMax && batch_fits(st, w * 2)) w *= 2;
+  return w;
+}
+
 // Tables of one complex core as the batch kernel runs it.
 struct HostCore {
   BatchCore d{};
@@ -380,15 +389,16 @@ int chfft_batch_create(int dtype, const chfft_batch_job* jobs, size_t njobs, chf
           work_elems += hb.m;
         }
         // tasks of this item
-        const int na = (hb.fs.n2 + kBatchTile - 1) / kBatchTile, nb = (hb.fs.n1 + kBatchTile - 1) / kBatchTile;
+        const int wa = fs_width(hb.ca.d.st), wb = fs_width(hb.cb.d.st);
+        const int na = (hb.fs.n2 + wa - 1) / wa, nb = (hb.fs.n1 + wb - 1) / wb;
         const int c0 = nctr;
         nctr += 4;
-        for (int t = 0; t < na; t++) lv[0].push_back({BT_FS_A, (int)i, 1, hb.blue ? 1 : 0, t, -1, 0, c0});
+        for (int t = 0; t < na; t++) lv[0].push_back({BT_FS_A, (int)i, wa, hb.blue ? 1 : 0, t, -1, 0, c0});
         const int bmode = hb.blue ? 1 : (x.kind == BK_C2C ? 0 : 3);
-        for (int t = 0; t < nb; t++) lv[1].push_back({BT_FS_B, (int)i, 1, bmode, t, c0, na, c0 + 1});
+        for (int t = 0; t < nb; t++) lv[1].push_back({BT_FS_B, (int)i, wb, bmode, t, c0, na, c0 + 1});
         if (hb.blue) {
-          for (int t = 0; t < na; t++) lv[2].push_back({BT_FS_A, (int)i, 1, 2, t, c0 + 1, nb, c0 + 2});
-          for (int t = 0; t < nb; t++) lv[3].push_back({BT_FS_B, (int)i, 1, 2, t, c0 + 2, na, c0 + 3});
+          for (int t = 0; t < na; t++) lv[2].push_back({BT_FS_A, (int)i, wa, 2, t, c0 + 1, nb, c0 + 2});
+          for (int t = 0; t < nb; t++) lv[3].push_back({BT_FS_B, (int)i, wb, 2, t, c0 + 2, na, c0 + 3});
         }
         if (x.kind != BK_C2C) {
           const int pairs = (int)((x.n + 3) / 4);
@@ -429,8 +439,8 @@ int chfft_batch_create(int dtype, const chfft_batch_job* jobs, size_t njobs, chf
       const BatchItem& it = items[t.item];
       size_t need = 0;
       if (t.type == BT_SMALL) need = (size_t)t.count * smem_ld(it.core.st.n) * 8;
-      else if (t.type == BT_FS_A) need = (size_t)kBatchTile * smem_ld(it.ca.st.n) * 8;
-      else if (t.type == BT_FS_B) need = (size_t)kBatchTile * smem_ld(it.cb.st.n) * 8;
+      else if (t.type == BT_FS_A) need = (size_t)t.count * smem_ld(it.ca.st.n) * 8;
+      else if (t.type == BT_FS_B) need = (size_t)t.count * smem_ld(it.cb.st.n) * 8;
       smem = std::max(smem, need);
     }
     // ---- upload

@@ -149,11 +149,9 @@ int tile_ld(const StageList& st, int tpb, int dtype, bool column) {
   return ld;
 }
 
-std::string name_expression(Kernel k, int dtype, const Core& c, const StageList& sl, const Geo& g, int mode) {
-  std::string s = "&";
-  s += kernel_template(k);
-  s += dtype == 0 ? "<float, " : "<double, ";
-  s += "chfft::StatCore<";
+// "chfft::StatCore<...>" of a specialised kernel.
+std::string core_expression(Kernel k, int dtype, const Core& c, const StageList& sl, const Geo& g) {
+  std::string s = "chfft::StatCore<";
   s += c.blue ? "true," : "false,";
   s += column_mapped(k) ? "true," : "false,";
   s += g.k1 ? "true," : "false,";
@@ -171,6 +169,14 @@ std::string name_expression(Kernel k, int dtype, const Core& c, const StageList&
        std::to_string(g.k1 ? 0 : g.ept);
   for (int r : pass_order(sl)) s += "," + std::to_string(r);
   s += ">";
+  return s;
+}
+
+std::string name_expression(Kernel k, int dtype, const Core& c, const StageList& sl, const Geo& g, int mode) {
+  std::string s = "&";
+  s += kernel_template(k);
+  s += dtype == 0 ? "<float, " : "<double, ";
+  s += core_expression(k, dtype, c, sl, g);
   if (four_step(k)) s += ", " + std::to_string(mode);
   s += ">";
   return s;
@@ -236,12 +242,19 @@ bool jit_available(std::string* why) {
   return ok;
 }
 
-int jit_launch(Kernel k, int dtype, const Core& c, const Geo& g0, const KArgs& a0, unsigned blocks,
-               cudaStream_t stream, int mode, const FourStep* fs) {
-  if (four_step(k) && !fs) return 1;
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (!load_api()) return 1;
-  if (!c.stw.p) return 1;
+namespace {
+
+// Geometry, stage list and arguments of a specialised launch.
+struct Spec {
+  Geo g;
+  const StageList* sl = nullptr;
+  KArgs a;
+};
+
+// False when the core has no specialised form for this geometry.
+bool resolve(Kernel k, int dtype, const Core& c, const Geo& g0, const KArgs& a0, int mode, const FourStep* fs,
+             Spec* out) {
+  if (!c.stw.p) return false;
   // Stage list: the radix-32 one where every thread holds 32 elements.
   const bool wide = !g0.k1 && g0.ept == 0 && g0.max_radix >= 32 && c.wide.p;
   const StageList& sl = wide ? c.sw : c.st;
@@ -269,22 +282,29 @@ int jit_launch(Kernel k, int dtype, const Core& c, const Geo& g0, const KArgs& a
   g.smem = (size_t)g.tpb * g.ld * cplx_bytes(dtype);
   if (k == Kernel::COLS_TW && (mode & 8) && fs)  // pass A's twiddle tables after the tile
     g.smem = (g.smem + 15) / 16 * 16 + (size_t)smem_twiddle_entries(g.tpb, fs->n1) * cplx_bytes(dtype);
-  if (g.smem > kMaxSmem) return 1;
+  if (g.smem > kMaxSmem) return false;
   if (wide) {
     int th = threads_needed(sl, ept_of(dtype), g.tpb, false);
     th = std::max(32, ((th + 31) / 32) * 32);
-    if (th > kMaxThreads) return 1;
+    if (th > kMaxThreads) return false;
     g.threads = th;
   }
-  KArgs a = a0;
-  a.ld = g.ld;
+  out->a = a0;
+  out->a.ld = g.ld;
   if (wide) {
-    a.core.st = sl;
-    a.core.stw = c.wide.p;
+    out->a.core.st = sl;
+    out->a.core.stw = c.wide.p;
   }
+  out->g = g;
+  out->sl = &sl;
+  return true;
+}
+
+// The compiled kernel for expr with at least smem bytes of dynamic shared
+// memory allowed (caller holds g_mu). Returns 0, 1 (unavailable) or 2.
+int kernel_for(const std::string& expr, size_t smem, CUfunction* fn) {
   int dev = 0;
   cudaGetDevice(&dev);
-  const std::string expr = name_expression(k, dtype, c, sl, g, mode);
   Entry& e = g_cache[std::to_string(dev) + "|" + expr];
   if (e.failed) return 1;
   if (!e.fn) {
@@ -295,22 +315,68 @@ int jit_launch(Kernel k, int dtype, const Core& c, const Geo& g0, const KArgs& a
       return 1;
     }
   }
-  if ((int)g.smem > 48 * 1024 && e.smem_set < (int)g.smem) {
-    if (g_api.cuFuncSetAttribute(e.fn, kAttrMaxDynSmem, (int)g.smem) != 0) return 2;
-    e.smem_set = (int)g.smem;
+  if ((int)smem > 48 * 1024 && e.smem_set < (int)smem) {
+    if (g_api.cuFuncSetAttribute(e.fn, kAttrMaxDynSmem, (int)smem) != 0) return 2;
+    e.smem_set = (int)smem;
   }
+  *fn = e.fn;
+  return 0;
+}
+
+}  // namespace
+
+int jit_launch(Kernel k, int dtype, const Core& c, const Geo& g0, const KArgs& a0, unsigned blocks,
+               cudaStream_t stream, int mode, const FourStep* fs) {
+  if (four_step(k) && !fs) return 1;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!load_api()) return 1;
+  Spec sp;
+  if (!resolve(k, dtype, c, g0, a0, mode, fs, &sp)) return 1;
+  const Geo& g = sp.g;
+  KArgs& a = sp.a;
+  CUfunction fn = nullptr;
+  const std::string expr = name_expression(k, dtype, c, *sp.sl, g, mode);
+  if (int r = kernel_for(expr, g.smem, &fn)) return r;
   // L2 prefetch of the next wave's input (rows, columns, four-step passes).
   const bool prefetching = k == Kernel::C2C || k == Kernel::COLS || four_step(k);
   a.ahead = 0;
   if (prefetching && g.prefetch > 0) {
     int per_sm = 0;
-    if (g_api.cuOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, e.fn, g.threads, g.smem) == 0 && per_sm > 0) {
+    if (g_api.cuOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, g.threads, g.smem) == 0 && per_sm > 0) {
       const long long resident = (long long)per_sm * num_sms();
       if (g.prefetch > 0 || (long long)blocks > resident) a.ahead = resident;
     }
   }
   void* args[] = {const_cast<KArgs*>(&a), const_cast<FourStep*>(fs)};
-  if (g_api.cuLaunchKernel(e.fn, blocks, 1, 1, g.threads, 1, 1, (unsigned)g.smem, (CUstream)stream, args, nullptr) != 0)
+  if (g_api.cuLaunchKernel(fn, blocks, 1, 1, g.threads, 1, 1, (unsigned)g.smem, (CUstream)stream, args, nullptr) != 0)
+    return 2;
+  return 0;
+}
+
+int jit_launch_fused(const Core& ca, const Geo& ga0, const KArgs& a0, int mode_a, const Core& cb, const Geo& gb0,
+                     const KArgs& b0, int mode_b, const FourStep& fs, FusedSched f, cudaStream_t stream) {
+  if (ca.dtype != cb.dtype || ca.blue || cb.blue) return 1;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!load_api()) return 1;
+  Spec sa, sb;
+  if (!resolve(Kernel::COLS_TW, ca.dtype, ca, ga0, a0, mode_a, &fs, &sa) ||
+      !resolve(Kernel::ROWS_T, cb.dtype, cb, gb0, b0, mode_b, &fs, &sb))
+    return 1;
+  if (sa.g.threads != sb.g.threads) return 1;
+  const size_t smem = std::max(sa.g.smem, sb.g.smem);
+  std::string expr = "&chfft::kern::k_fourstep_fused<";
+  expr += ca.dtype == 0 ? "float, " : "double, ";
+  expr += core_expression(Kernel::COLS_TW, ca.dtype, ca, *sa.sl, sa.g) + ", ";
+  expr += core_expression(Kernel::ROWS_T, cb.dtype, cb, *sb.sl, sb.g) + ", ";
+  expr += std::to_string(mode_a) + ", " + std::to_string(mode_b) + ">";
+  CUfunction fn = nullptr;
+  if (int r = kernel_for(expr, smem, &fn)) return r;
+  const long long tasks = f.count * (f.tiles_a + (long long)f.tiles_b);
+  if (tasks > 0x7fffffffLL) return 1;
+  const unsigned blocks = (unsigned)tasks;
+  sa.a.ahead = sb.a.ahead = 0;
+  void* args[] = {&sa.a, &sb.a, const_cast<FourStep*>(&fs), &f};
+  if (g_api.cuLaunchKernel(fn, blocks, 1, 1, sa.g.threads, 1, 1, (unsigned)smem, (CUstream)stream, args, nullptr) != 0)
     return 2;
   return 0;
 }

@@ -153,7 +153,9 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_batch(const BatchArgs A) {
     // ---- the core and its tile
     const BatchCore& core = tk.type == BT_SMALL ? it.core : (tk.type == BT_FS_A ? it.ca : it.cb);
     const int m = core.st.n;
-    const int tpb = tk.type == BT_SMALL ? tk.count : kBatchTile;
+    // SMALL: transforms in the task; FS_A / FS_B: tile width (a power of two).
+    const int tpb = tk.count;
+    const int lw = 31 - __clz(tpb);
     const SmemIO<C> sm{sbase, smem_ld(m)};
     const FourStep& fs = it.fs;
 
@@ -173,9 +175,9 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_batch(const BatchArgs A) {
         sm.store(t, i, v);
       }
     } else if (tk.type == BT_FS_A) {
-      const int c0 = tk.tile * kBatchTile;
+      const int c0 = tk.tile * tpb;
       for (int b = tid; b < tpb * m; b += nth) {
-        const int t = b % kBatchTile, i = b / kBatchTile;  // consecutive threads: adjacent columns
+        const int t = b & (tpb - 1), i = b >> lw;  // consecutive threads: adjacent columns
         const int col = c0 + t;
         C v = czero<C>();
         if (col < fs.n2) {
@@ -194,7 +196,7 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_batch(const BatchArgs A) {
         sm.store(t, i, v);
       }
     } else {  // BT_FS_B
-      const int r0 = tk.tile * kBatchTile;
+      const int r0 = tk.tile * tpb;
       const C* w = reinterpret_cast<const C*>(A.work + it.work_off);
       for (int b = tid; b < tpb * m; b += nth) {
         const int t = b / m, i = b - t * m;  // consecutive threads along a row
@@ -243,12 +245,12 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_batch(const BatchArgs A) {
         }
       }
     } else if (tk.type == BT_FS_A) {
-      const int c0 = tk.tile * kBatchTile;
+      const int c0 = tk.tile * tpb;
       C* w = reinterpret_cast<C*>(A.work + it.work_off);
       const C* lo = static_cast<const C*>(fs.lo);
       const C* hi = static_cast<const C*>(fs.hi);
       for (int b = tid; b < tpb * m; b += nth) {
-        const int t = b % kBatchTile, k1 = b / kBatchTile;
+        const int t = b & (tpb - 1), k1 = b >> lw;
         const int col = c0 + t;
         if (col >= fs.n2) continue;
         const long long e = (long long)k1 * col;
@@ -256,9 +258,9 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_batch(const BatchArgs A) {
         w[(long long)k1 * fs.n2 + col] = cmul(sm.load(t, k1), tw);
       }
     } else {  // BT_FS_B: X[k1 + n1 k2]
-      const int r0 = tk.tile * kBatchTile;
+      const int r0 = tk.tile * tpb;
       for (int b = tid; b < tpb * m; b += nth) {
-        const int t = b % kBatchTile, k2 = b / kBatchTile;  // consecutive threads: adjacent k1
+        const int t = b & (tpb - 1), k2 = b >> lw;  // consecutive threads: adjacent k1
         const int row = r0 + t;
         if (row >= fs.n1) continue;
         const long long k = row + (long long)fs.n1 * k2;

@@ -4,9 +4,9 @@
 // Task types
 //   SMALL  `count` consecutive transforms of one kind and length, whole in
 //          one CTA (C2C, R2C, DCT-II, MDCT; mixed radix or Bluestein core)
-//   FS_A   four-step column tile: 16 columns of length n1, pre-processing of
+//   FS_A   four-step column tile: 16-64 columns of length n1, pre-processing of
 //          the kind fused into the load, w_m^(k1 n2) into the store
-//   FS_B   four-step row tile: 16 rows of length n2, transposed store (plain,
+//   FS_B   four-step row tile: 16-64 rows of length n2, transposed store (plain,
 //          Bluestein spectrum, Bluestein chirp-out, or the core output of a
 //          real kind for its POST tasks)
 //   POST   the R2C split / DCT-II post-twiddle of a four-step real kind
@@ -23,7 +23,8 @@ namespace chfft {
 
 constexpr int kBatchThreads = 512;
 constexpr int kBatchEpt = 16;   // complex elements per thread per pass (64 registers)
-constexpr int kBatchTile = 16;  // four-step tile width (columns / rows)
+constexpr int kBatchTile = 16;     // narrowest four-step tile (columns / rows)
+constexpr int kBatchTileMax = 64;  // widest four-step tile
 
 enum BatchKind : int { BK_C2C = 0, BK_R2C = 1, BK_DCT2 = 2, BK_MDCT = 3 };
 enum BatchTaskType : int { BT_SMALL = 0, BT_FS_A = 1, BT_FS_B = 2, BT_POST = 3 };
@@ -58,7 +59,7 @@ struct BatchItem {
 struct BatchTask {
   int type;         // BatchTaskType
   int item;         // first item
-  int count;        // SMALL: consecutive items of the same kind / length
+  int count;        // SMALL: consecutive items of the same kind / length; FS_A / FS_B: tile width
   int mode;         // FS_A: 0 plain, 1 chirp in; FS_B: 0 out, 1 spectrum, 2 chirp out, 3 core out (real kinds)
   int tile;         // FS_A / FS_B tile, POST chunk
   int wait_ctr, wait_target, signal_ctr;

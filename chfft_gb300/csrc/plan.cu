@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 
 #include "../../include/chfft_gpu.h"
@@ -503,7 +504,8 @@ long long BigCore::chunk(long long batch) const {
   return std::max(1LL, std::min(batch, (budget_mb << 20) / per));
 }
 
-long long BigCore::work_elems(long long batch) const { return chunk(batch) * m * (blue ? 2 : 1); }
+// Plus 64 KiB (f32) for the fused launch's counters.
+long long BigCore::work_elems(long long batch) const { return chunk(batch) * m * (blue ? 2 : 1) + 8192; }
 
 void BigCore::exec(const void* in, void* out, void* work, long long batch, bool back, double scale,
                    cudaStream_t s, long long max_chunk, bool library_only) const {
@@ -527,6 +529,60 @@ void BigCore::exec(const void* in, void* out, void* work, long long batch, bool 
     gb.tpb = tile(cb, Kernel::ROWS_T);
     if (!ga.tpb || !gb.tpb)
       throw Fail{CHFFT_EUNSUPPORTED, "tensor-core passes need power-of-two four-step factors >= 16"};
+  }
+  // Both passes in one launch over a ring of L2-resident intermediates
+  // (plain f32 four-step, specialised kernels; CHFFT_FUSED="lead,ring,hints").
+  int lead = 0, ring = 0, hints = 1;
+  if (const char* e = std::getenv("CHFFT_FUSED")) std::sscanf(e, "%d,%d,%d", &lead, &ring, &hints);
+  if (lead > 0 && !blue && dtype == 0 && tc <= 0 && !library_only && max_chunk <= 0 &&
+      want_specialised(batch * m, opts.jit)) {
+    lead = (int)std::min<long long>(lead, batch);
+    ring = (int)std::min<long long>(std::max(ring, lead + 1), batch);
+    const size_t ctr_bytes = 16 + 8 * (size_t)batch;
+    if ((size_t)ring * m * cb_ + ctr_bytes <= (size_t)work_elems(batch) * cb_) {
+      char* ctr = tmp + (size_t)ring * m * cb_;
+      CHFFT_CUDA(cudaMemsetAsync(ctr, 0, ctr_bytes, s));
+      FusedSched fz{};
+      fz.next = reinterpret_cast<unsigned long long*>(ctr);
+      fz.err = reinterpret_cast<int*>(ctr + 8);
+      fz.done_a = reinterpret_cast<int*>(ctr + 16);
+      fz.done_b = fz.done_a + batch;
+      fz.count = batch;
+      fz.tiles_a = (n2 + ga.tpb - 1) / ga.tpb;
+      fz.tiles_b = (n1 + gb.tpb - 1) / gb.tpb;
+      fz.lead = lead;
+      fz.ring = ring;
+      fz.spin_limit = 4000000;  // ~1 s
+      KArgs a{}, b{};
+      a.core = ca.desc();
+      a.tpb = ga.tpb;
+      a.ld = ga.ld;
+      a.back = back;
+      a.count = batch;
+      a.tiles_per_tr = fz.tiles_a;
+      a.in = in;
+      a.out = tmp;
+      a.scale = scale;
+      a.in_dist = n;
+      a.out_dist = m;
+      a.ncols = n2;
+      b.core = cb.desc();
+      b.tpb = gb.tpb;
+      b.ld = gb.ld;
+      b.back = back;
+      b.count = batch;
+      b.tiles_per_tr = fz.tiles_b;
+      b.in = tmp;
+      b.out = out;
+      b.scale = 1.0;
+      b.in_dist = m;
+      b.out_dist = n;
+      b.ncols = n2;
+      const int hb = hints ? 4 : 0;
+      const int r = jit_launch_fused(ca, ga, a, hb | 8, cb, gb, b, hb, f, fz, s);
+      if (r == 2) throw Fail{CHFFT_ECUDA, "launch of the fused four-step kernel failed"};
+      if (r == 0) return;
+    }
   }
   for (long long c0 = 0; c0 < batch; c0 += g) {
     const long long cnt = std::min(g, batch - c0);
