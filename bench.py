@@ -503,7 +503,7 @@ def run_uneven(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uniform[-1,1))",
         "config": {"workload": "uneven batch: 10000 jobs, lengths log-uniform [16, 65536], 60% C2C (15% of all prime), "
-                               "20% RFft1D, 10% DCT-II, 10% MDCT 2048 sine; one persistent launch in a CUDA graph",
+                               "20% RFft1D, 10% DCT-II, 10% MDCT 2048 sine; one work-queue launch in a CUDA graph",
                    "l2": "flushed between timed steps", "tasks": info.tasks, "ctas": info.ctas,
                    "four_step_lengths": info.four_step_lengths, "one_cta_lengths": info.one_cta_lengths},
         "hbm_gbs": round(nbytes / (ms * 1e-3) / 1e9, 1),

@@ -506,7 +506,7 @@ def pack_jobs(specs, align: int = 16):
 
 
 class Batch:
-    """Uneven batch: many f32 forward transforms in one persistent launch."""
+    """Uneven batch: many f32 forward transforms in one work-queue launch."""
 
     def __init__(self, specs, dtype=np.float32):
         L = lib()

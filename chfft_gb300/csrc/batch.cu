@@ -1,5 +1,6 @@
-// Uneven batches: many transforms of mixed kinds and lengths in one
-// persistent launch (k_batch.cu), optionally replayed from a CUDA graph.
+// Uneven batches: many transforms of mixed kinds and lengths in one launch
+// fed by a device task queue (k_batch.cu), optionally replayed from a CUDA
+// graph.
 //
 // The host side groups the jobs by (kind, length, option), builds each
 // distinct length's tables once (FP64-generated, like every plan), decides
@@ -11,6 +12,7 @@
 // replayed.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -25,7 +27,7 @@
 namespace chfft {
 
 int record_error(int code, const std::string& msg);
-cudaError_t launch_batch(const BatchArgs& a, unsigned blocks, size_t smem, cudaStream_t stream);
+cudaError_t launch_batch(const BatchArgs& a, unsigned blocks, size_t smem, cudaStream_t stream, bool persist);
 int batch_blocks_per_sm(size_t smem);
 
 namespace {
@@ -203,7 +205,8 @@ struct BatchImpl {
   DevBuf d_items, d_tasks, d_ctr, d_work;
   int ntasks = 0, nitems = 0, nctr = 0, nbig = 0;
   size_t smem = 0, work_bytes = 0;
-  unsigned blocks = 0;
+  unsigned blocks = 0;  // CTAs per launch
+  bool persist = false;  // resident CTAs looping over the queue (else one CTA per task)
   cudaStream_t stream = nullptr;
   // captured launch
   cudaGraph_t graph = nullptr;
@@ -231,7 +234,7 @@ struct BatchImpl {
     a.out = static_cast<char*>(d_out);
     a.work = static_cast<char*>(d_work.p);
     a.spin_limit = 10 * 1000 * 1000;  // x 200 ns: ~2 s before a wait gives up
-    CHFFT_CUDA(launch_batch(a, blocks, smem, s));
+    CHFFT_CUDA(launch_batch(a, blocks, smem, s, persist));
   }
 };
 
@@ -461,7 +464,10 @@ int chfft_batch_create(int dtype, const chfft_batch_job* jobs, size_t njobs, chf
     CHFFT_CUDA(cudaGetDevice(&dev));
     CHFFT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const int per_sm = batch_blocks_per_sm(smem);
-    B.blocks = (unsigned)std::max(1, std::min(per_sm * sms, std::max(1, B.ntasks)));
+    const char* pe = std::getenv("CHFFT_BATCH_PERSISTENT");
+    B.persist = pe && *pe && std::strcmp(pe, "0") != 0;
+    B.blocks = B.persist ? (unsigned)std::max(1, std::min(per_sm * sms, std::max(1, B.ntasks)))
+                         : (unsigned)std::max(1, B.ntasks);
     CHFFT_CUDA(cudaStreamSynchronize(s));
   } catch (const Fail& f) {
     return record_error(f.code, f.msg);

@@ -117,186 +117,215 @@ __device__ __forceinline__ void signal(const BatchArgs& A, int ctr) {
   }
 }
 
+// One task of the queue, ticket ti (s_item: the CTA's descriptor copy).
+template <bool PERSIST>
+__device__ __forceinline__ void batch_task(const BatchArgs& A, int ti, unsigned char* smem_raw, BatchItem& s_item) {
+  C* sbase = reinterpret_cast<C*>(smem_raw);
+  const BatchTask tk = A.tasks[ti];
+  {
+    const int* src = reinterpret_cast<const int*>(A.items + tk.item);
+    int* dst = reinterpret_cast<int*>(&s_item);
+    for (int w = threadIdx.x; w < (int)(sizeof(BatchItem) / 4); w += blockDim.x) dst[w] = __ldg(src + w);
+  }
+  if (tk.wait_ctr >= 0) wait_for(A, tk.wait_ctr, tk.wait_target);  // ends with a barrier
+  else __syncthreads();
+  const BatchItem& it = s_item;
+  const int tid = threadIdx.x, nth = blockDim.x;
+
+  if (tk.type == BT_POST) {
+    const C* z = reinterpret_cast<const C*>(A.work + it.work2_off);
+    const int i = tk.tile * kPostChunk;
+    for (int p = i + tid; p < i + kPostChunk; p += nth) real_post(it, A.out, p, [&](int k) { return ldcg(z + k); });
+    if (tk.signal_ctr >= 0) signal(A, tk.signal_ctr);
+    return;
+  }
+
+  // ---- the core and its tile
+  const BatchCore& core = tk.type == BT_SMALL ? it.core : (tk.type == BT_FS_A ? it.ca : it.cb);
+  const int m = core.st.n;
+  // SMALL: transforms in the task; FS_A / FS_B: tile width (a power of two).
+  const int tpb = tk.count;
+  const int lw = 31 - __clz(tpb);
+  const SmemIO<C> sm{sbase, smem_ld(m)};
+  const FourStep& fs = it.fs;
+
+  // ---- load phase
+  if (tk.type == BT_SMALL) {
+    for (int b = tid; b < tpb * m; b += nth) {
+      const int t = b / m, i = b - t * m;
+      const BatchItem& x = A.items[tk.item + t];
+      C v = czero<C>();
+      if (i < core.n) {
+        if (x.kind == BK_C2C)
+          v = cscale(reinterpret_cast<const C*>(A.in + x.in_off)[i], x.scale);
+        else
+          v = real_pre(x, A.in, i);
+        if (core.blue) v = cmul(v, __ldg(&static_cast<const C*>(core.chirp)[i]));
+      }
+      sm.store(t, i, v);
+    }
+  } else if (tk.type == BT_FS_A) {
+    const int c0 = tk.tile * tpb;
+    for (int b = tid; b < tpb * m; b += nth) {
+      const int t = b & (tpb - 1), i = b >> lw;  // consecutive threads: adjacent columns
+      const int col = c0 + t;
+      C v = czero<C>();
+      if (col < fs.n2) {
+        const long long flat = (long long)i * fs.n2 + col;
+        if (tk.mode == 2) {
+          v = ldcg(reinterpret_cast<const C*>(A.work + it.work2_off) + flat);
+        } else if (it.kind == BK_C2C) {
+          if (tk.mode == 0 || flat < fs.n_user) {
+            v = cscale(reinterpret_cast<const C*>(A.in + it.in_off)[flat], it.scale);
+            if (tk.mode == 1) v = cmul(v, __ldg(&static_cast<const C*>(fs.chirp)[flat]));
+          }
+        } else {
+          v = real_pre(it, A.in, flat);
+        }
+      }
+      sm.store(t, i, v);
+    }
+  } else {  // BT_FS_B
+    const int r0 = tk.tile * tpb;
+    const C* w = reinterpret_cast<const C*>(A.work + it.work_off);
+    for (int b = tid; b < tpb * m; b += nth) {
+      const int t = b / m, i = b - t * m;  // consecutive threads along a row
+      const int row = r0 + t;
+      sm.store(t, i, row < fs.n1 ? ldcg(w + (long long)row * fs.n2 + i) : czero<C>());
+    }
+  }
+  __syncthreads();
+
+  // ---- complex core (one call site for every task type)
+  if constexpr (PERSIST) {  // one call site inside the task loop
+    for (int r = 0; r < (core.blue ? 2 : 1); r++) {
+      if (r == 1) spectrum_phase<false>(sm, m, tpb, static_cast<const C*>(core.bhat));
+      smem_passes<false, false, kBatchEpt>(core.st.all, m, 1, tpb, static_cast<const C*>(core.tw), sm);
+    }
+  } else {
+    // Two call sites rather than a loop over the Bluestein rounds: a loop
+    // around the passes makes the compiler spill.
+    smem_passes<false, false, kBatchEpt>(core.st.all, m, 1, tpb, static_cast<const C*>(core.tw), sm);
+    if (core.blue) {
+      spectrum_phase<false>(sm, m, tpb, static_cast<const C*>(core.bhat));
+      smem_passes<false, false, kBatchEpt>(core.st.all, m, 1, tpb, static_cast<const C*>(core.tw), sm);
+    }
+  }
+
+  // ---- store phase
+  if (tk.type == BT_SMALL) {
+    const int L = core.n;
+    if (core.blue) {  // Z_k = conj(Y_k) c_k, in place
+      for (int b = tid; b < tpb * L; b += nth) {
+        const int t = b / L, k = b - t * L;
+        sm.store(t, k, cmul(cconj(sm.load(t, k)), __ldg(&static_cast<const C*>(core.chirp)[k])));
+      }
+      __syncthreads();
+    }
+    if (it.kind == BK_C2C || it.kind == BK_MDCT) {
+      for (int b = tid; b < tpb * L; b += nth) {
+        const int t = b / L, k = b - t * L;
+        const BatchItem& x = A.items[tk.item + t];
+        const C z = sm.load(t, k);
+        if (x.kind == BK_C2C) {
+          reinterpret_cast<C*>(A.out + x.out_off)[k] = z;
+        } else {
+          C r = cmul(z, cscale(__ldg(&static_cast<const C*>(x.aux0)[k]), x.scale));
+          float* o = reinterpret_cast<float*>(A.out + x.out_off);
+          o[2 * k] = -r.x;
+          o[(x.n >> 1) - 1 - 2 * k] = r.y;
+        }
+      }
+    } else {
+      const int pairs = (it.n + 3) >> 2;
+      for (int b = tid; b < tpb * pairs; b += nth) {
+        const int t = b / pairs, i = b - t * pairs;
+        real_post(A.items[tk.item + t], A.out, i, [&](int k) { return sm.load(t, k); });
+      }
+    }
+  } else if (tk.type == BT_FS_A) {
+    const int c0 = tk.tile * tpb;
+    C* w = reinterpret_cast<C*>(A.work + it.work_off);
+    const C* lo = static_cast<const C*>(fs.lo);
+    const C* hi = static_cast<const C*>(fs.hi);
+    for (int b = tid; b < tpb * m; b += nth) {
+      const int t = b & (tpb - 1), k1 = b >> lw;
+      const int col = c0 + t;
+      if (col >= fs.n2) continue;
+      const long long e = (long long)k1 * col;
+      const C tw = cmul(__ldg(&hi[e >> fs.tw_shift]), __ldg(&lo[e & ((1LL << fs.tw_shift) - 1)]));
+      w[(long long)k1 * fs.n2 + col] = cmul(sm.load(t, k1), tw);
+    }
+  } else {  // BT_FS_B: X[k1 + n1 k2]
+    const int r0 = tk.tile * tpb;
+    for (int b = tid; b < tpb * m; b += nth) {
+      const int t = b & (tpb - 1), k2 = b >> lw;  // consecutive threads: adjacent k1
+      const int row = r0 + t;
+      if (row >= fs.n1) continue;
+      const long long k = row + (long long)fs.n1 * k2;
+      const C v = sm.load(t, k2);
+      if (tk.mode == 0) {
+        reinterpret_cast<C*>(A.out + it.out_off)[k] = v;
+      } else if (tk.mode == 1) {
+        reinterpret_cast<C*>(A.work + it.work2_off)[k] = cconj(cmul(v, __ldg(&static_cast<const C*>(fs.bhat)[k])));
+      } else if (tk.mode == 2) {
+        if (k < fs.n_user)
+          reinterpret_cast<C*>(A.out + it.out_off)[k] =
+              cmul(cconj(v), __ldg(&static_cast<const C*>(fs.chirp)[k]));
+      } else {
+        reinterpret_cast<C*>(A.work + it.work2_off)[k] = v;
+      }
+    }
+  }
+  if (tk.signal_ctr >= 0) signal(A, tk.signal_ctr);
+}
+
+// PERSIST: resident CTAs loop over the queue. Otherwise one CTA per task,
+// each taking its ticket when it starts: a task then only waits on tickets
+// taken earlier by running CTAs, as in the looping form. Without the loop
+// the compiler keeps the pass code in registers (the loop made it spill
+// 836 bytes per thread).
+template <bool PERSIST>
 __global__ void __launch_bounds__(kBatchThreads, 2) k_batch(const BatchArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C* sbase = reinterpret_cast<C*>(smem_raw);
   __shared__ int s_task;
   // The task's item descriptor, copied once per task: its fields are read
   // all through the task, from shared memory instead of global memory.
   __shared__ __align__(16) BatchItem s_item;
   static_assert(sizeof(BatchItem) % 4 == 0, "item descriptor copied as 32-bit words");
-  for (;;) {
-    __syncthreads();
+  if constexpr (PERSIST) {
+    for (;;) {
+      __syncthreads();
+      if (threadIdx.x == 0) s_task = atomicAdd(A.next, 1);
+      __syncthreads();
+      const int ti = s_task;
+      if (ti >= A.ntasks) return;
+      batch_task<true>(A, ti, smem_raw, s_item);
+    }
+  } else {
     if (threadIdx.x == 0) s_task = atomicAdd(A.next, 1);
     __syncthreads();
     const int ti = s_task;
-    if (ti >= A.ntasks) return;
-    const BatchTask tk = A.tasks[ti];
-    {
-      const int* src = reinterpret_cast<const int*>(A.items + tk.item);
-      int* dst = reinterpret_cast<int*>(&s_item);
-      for (int w = threadIdx.x; w < (int)(sizeof(BatchItem) / 4); w += blockDim.x) dst[w] = __ldg(src + w);
-    }
-    if (tk.wait_ctr >= 0) wait_for(A, tk.wait_ctr, tk.wait_target);  // ends with a barrier
-    else __syncthreads();
-    const BatchItem& it = s_item;
-    const int tid = threadIdx.x, nth = blockDim.x;
-
-    if (tk.type == BT_POST) {
-      const C* z = reinterpret_cast<const C*>(A.work + it.work2_off);
-      const int i = tk.tile * kPostChunk;
-      for (int p = i + tid; p < i + kPostChunk; p += nth) real_post(it, A.out, p, [&](int k) { return ldcg(z + k); });
-      if (tk.signal_ctr >= 0) signal(A, tk.signal_ctr);
-      continue;
-    }
-
-    // ---- the core and its tile
-    const BatchCore& core = tk.type == BT_SMALL ? it.core : (tk.type == BT_FS_A ? it.ca : it.cb);
-    const int m = core.st.n;
-    // SMALL: transforms in the task; FS_A / FS_B: tile width (a power of two).
-    const int tpb = tk.count;
-    const int lw = 31 - __clz(tpb);
-    const SmemIO<C> sm{sbase, smem_ld(m)};
-    const FourStep& fs = it.fs;
-
-    // ---- load phase
-    if (tk.type == BT_SMALL) {
-      for (int b = tid; b < tpb * m; b += nth) {
-        const int t = b / m, i = b - t * m;
-        const BatchItem& x = A.items[tk.item + t];
-        C v = czero<C>();
-        if (i < core.n) {
-          if (x.kind == BK_C2C)
-            v = cscale(reinterpret_cast<const C*>(A.in + x.in_off)[i], x.scale);
-          else
-            v = real_pre(x, A.in, i);
-          if (core.blue) v = cmul(v, __ldg(&static_cast<const C*>(core.chirp)[i]));
-        }
-        sm.store(t, i, v);
-      }
-    } else if (tk.type == BT_FS_A) {
-      const int c0 = tk.tile * tpb;
-      for (int b = tid; b < tpb * m; b += nth) {
-        const int t = b & (tpb - 1), i = b >> lw;  // consecutive threads: adjacent columns
-        const int col = c0 + t;
-        C v = czero<C>();
-        if (col < fs.n2) {
-          const long long flat = (long long)i * fs.n2 + col;
-          if (tk.mode == 2) {
-            v = ldcg(reinterpret_cast<const C*>(A.work + it.work2_off) + flat);
-          } else if (it.kind == BK_C2C) {
-            if (tk.mode == 0 || flat < fs.n_user) {
-              v = cscale(reinterpret_cast<const C*>(A.in + it.in_off)[flat], it.scale);
-              if (tk.mode == 1) v = cmul(v, __ldg(&static_cast<const C*>(fs.chirp)[flat]));
-            }
-          } else {
-            v = real_pre(it, A.in, flat);
-          }
-        }
-        sm.store(t, i, v);
-      }
-    } else {  // BT_FS_B
-      const int r0 = tk.tile * tpb;
-      const C* w = reinterpret_cast<const C*>(A.work + it.work_off);
-      for (int b = tid; b < tpb * m; b += nth) {
-        const int t = b / m, i = b - t * m;  // consecutive threads along a row
-        const int row = r0 + t;
-        sm.store(t, i, row < fs.n1 ? ldcg(w + (long long)row * fs.n2 + i) : czero<C>());
-      }
-    }
-    __syncthreads();
-
-    // ---- complex core (one call site for every task type)
-    const int rounds = core.blue ? 2 : 1;
-    for (int r = 0; r < rounds; r++) {
-      if (r == 1) spectrum_phase<false>(sm, m, tpb, static_cast<const C*>(core.bhat));
-      smem_passes<false, false, kBatchEpt>(core.st.all, m, 1, tpb, static_cast<const C*>(core.tw), sm);
-    }
-
-    // ---- store phase
-    if (tk.type == BT_SMALL) {
-      const int L = core.n;
-      if (core.blue) {  // Z_k = conj(Y_k) c_k, in place
-        for (int b = tid; b < tpb * L; b += nth) {
-          const int t = b / L, k = b - t * L;
-          sm.store(t, k, cmul(cconj(sm.load(t, k)), __ldg(&static_cast<const C*>(core.chirp)[k])));
-        }
-        __syncthreads();
-      }
-      if (it.kind == BK_C2C || it.kind == BK_MDCT) {
-        for (int b = tid; b < tpb * L; b += nth) {
-          const int t = b / L, k = b - t * L;
-          const BatchItem& x = A.items[tk.item + t];
-          const C z = sm.load(t, k);
-          if (x.kind == BK_C2C) {
-            reinterpret_cast<C*>(A.out + x.out_off)[k] = z;
-          } else {
-            C r = cmul(z, cscale(__ldg(&static_cast<const C*>(x.aux0)[k]), x.scale));
-            float* o = reinterpret_cast<float*>(A.out + x.out_off);
-            o[2 * k] = -r.x;
-            o[(x.n >> 1) - 1 - 2 * k] = r.y;
-          }
-        }
-      } else {
-        const int pairs = (it.n + 3) >> 2;
-        for (int b = tid; b < tpb * pairs; b += nth) {
-          const int t = b / pairs, i = b - t * pairs;
-          real_post(A.items[tk.item + t], A.out, i, [&](int k) { return sm.load(t, k); });
-        }
-      }
-    } else if (tk.type == BT_FS_A) {
-      const int c0 = tk.tile * tpb;
-      C* w = reinterpret_cast<C*>(A.work + it.work_off);
-      const C* lo = static_cast<const C*>(fs.lo);
-      const C* hi = static_cast<const C*>(fs.hi);
-      for (int b = tid; b < tpb * m; b += nth) {
-        const int t = b & (tpb - 1), k1 = b >> lw;
-        const int col = c0 + t;
-        if (col >= fs.n2) continue;
-        const long long e = (long long)k1 * col;
-        const C tw = cmul(__ldg(&hi[e >> fs.tw_shift]), __ldg(&lo[e & ((1LL << fs.tw_shift) - 1)]));
-        w[(long long)k1 * fs.n2 + col] = cmul(sm.load(t, k1), tw);
-      }
-    } else {  // BT_FS_B: X[k1 + n1 k2]
-      const int r0 = tk.tile * tpb;
-      for (int b = tid; b < tpb * m; b += nth) {
-        const int t = b & (tpb - 1), k2 = b >> lw;  // consecutive threads: adjacent k1
-        const int row = r0 + t;
-        if (row >= fs.n1) continue;
-        const long long k = row + (long long)fs.n1 * k2;
-        const C v = sm.load(t, k2);
-        if (tk.mode == 0) {
-          reinterpret_cast<C*>(A.out + it.out_off)[k] = v;
-        } else if (tk.mode == 1) {
-          reinterpret_cast<C*>(A.work + it.work2_off)[k] = cconj(cmul(v, __ldg(&static_cast<const C*>(fs.bhat)[k])));
-        } else if (tk.mode == 2) {
-          if (k < fs.n_user)
-            reinterpret_cast<C*>(A.out + it.out_off)[k] =
-                cmul(cconj(v), __ldg(&static_cast<const C*>(fs.chirp)[k]));
-        } else {
-          reinterpret_cast<C*>(A.work + it.work2_off)[k] = v;
-        }
-      }
-    }
-    if (tk.signal_ctr >= 0) signal(A, tk.signal_ctr);
+    if (ti < A.ntasks) batch_task<false>(A, ti, smem_raw, s_item);
   }
 }
 
 }  // namespace
 
-cudaError_t launch_batch(const BatchArgs& a, unsigned blocks, size_t smem, cudaStream_t stream) {
+cudaError_t launch_batch(const BatchArgs& a, unsigned blocks, size_t smem, cudaStream_t stream, bool persist) {
+  auto fn = persist ? k_batch<true> : k_batch<false>;
   if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  k_batch<<<blocks, kBatchThreads, smem, stream>>>(a);
+  fn<<<blocks, kBatchThreads, smem, stream>>>(a);
   return cudaGetLastError();
 }
 
 int batch_blocks_per_sm(size_t smem) {
   int n = 0;
-  if (smem > 48 * 1024) cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch, kBatchThreads, smem) != cudaSuccess) return 1;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(k_batch<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch<true>, kBatchThreads, smem) != cudaSuccess) return 1;
   return n > 0 ? n : 1;
 }
 

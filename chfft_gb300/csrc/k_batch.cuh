@@ -1,5 +1,6 @@
-// Persistent uneven-batch kernel: one launch runs a whole list of tasks of
-// mixed kinds and lengths, taken in order from a device work queue.
+// Uneven-batch kernel: one launch runs a whole list of tasks of mixed kinds
+// and lengths, taken in order from a device work queue (one task per CTA by
+// ticket, or resident CTAs looping over the queue).
 //
 // Task types
 //   SMALL  `count` consecutive transforms of one kind and length, whole in

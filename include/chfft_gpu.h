@@ -162,8 +162,9 @@ CHFFT_API int chfft_execute_device_noalloc(chfft_plan plan, int method, const vo
 
 /* ---- uneven batches ------------------------------------------------------ */
 
-/* Many transforms of mixed kinds and lengths in one persistent launch fed by
- * a device work queue. No counterpart in the reference (one chfft call is one
+/* Many transforms of mixed kinds and lengths in one launch fed by a device
+ * work queue (CTAs take tasks by ticket: one task per CTA, or, with
+ * CHFFT_BATCH_PERSISTENT=1 at create time, resident CTAs looping). No counterpart in the reference (one chfft call is one
  * transform); each job means the reference call `plan.method(&src)` of its
  * kind at its length. Jobs are f32 forward methods of CFft1D, RFft1D, Dct1D
  * (DCT-II) and Mdct1D; lengths from 2 up to 2^18 (C2C) and a 7-smooth half
@@ -182,7 +183,7 @@ typedef struct chfft_batch_s* chfft_batch;
 
 typedef struct chfft_batch_info {
   size_t jobs, tasks;
-  unsigned ctas;              /* persistent CTAs per launch */
+  unsigned ctas;              /* CTAs per launch */
   size_t smem_per_cta;
   size_t workspace_bytes;     /* four-step intermediates */
   size_t four_step_lengths, one_cta_lengths;
@@ -190,7 +191,7 @@ typedef struct chfft_batch_info {
 
 /* Builds every table and the task queue (device memory). */
 CHFFT_API int chfft_batch_create(int dtype, const chfft_batch_job* jobs, size_t njobs, chfft_batch* out);
-/* One persistent launch on `stream`: d_in / d_out are the bases the job
+/* One launch on `stream`: d_in / d_out are the bases the job
  * offsets refer to. Asynchronous. */
 CHFFT_API int chfft_batch_execute(chfft_batch batch, const void* d_in, void* d_out, void* stream);
 /* The same launch captured once into a CUDA graph (re-captured when the base

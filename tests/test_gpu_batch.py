@@ -1,4 +1,4 @@
-"""Uneven batches: one persistent launch over mixed kinds and lengths.
+"""Uneven batches: one work-queue launch over mixed kinds and lengths.
 
 Every job's output is checked against the oracle (the reference's call for
 that kind and length) at the f32 tolerance (relative L2 <= 5e-6 against the
