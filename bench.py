@@ -393,6 +393,32 @@ def uneven_specs(count=10000, seed=4):
     return specs
 
 
+def _smooth7(n):
+    for p in (2, 3, 5, 7):
+        while n % p == 0:
+            n //= p
+    return n == 1
+
+
+def uneven_subset(specs, name):
+    """One class of the uneven workload (profiling): 'small' = one-CTA jobs
+    (complex core <= 8192), 'big_c2c' / 'big_prime' = four-step C2C smooth /
+    prime, 'big_real' = four-step real kinds, 'all' = everything."""
+    if name == "all":
+        return specs
+
+    def core(k, n):
+        return n if k == "cfft1d" else n // 2 if k in ("rfft1d", "dct1d") else n // 4
+
+    keep = {
+        "small": lambda k, n: core(k, n) <= 8192,
+        "big_c2c": lambda k, n: k == "cfft1d" and core(k, n) > 8192 and _smooth7(n),
+        "big_prime": lambda k, n: k == "cfft1d" and core(k, n) > 8192 and not _smooth7(n),
+        "big_real": lambda k, n: k != "cfft1d" and core(k, n) > 8192,
+    }[name]
+    return [s for s in specs if keep(s[0], s[1])]
+
+
 def spec_flops(kind, n):
     return (5.0 if kind == "cfft1d" else 2.5) * n * math.log2(n)
 
@@ -440,7 +466,7 @@ def run_uneven(args):
 
     import chfft_gb300 as cg
 
-    specs = uneven_specs()
+    specs = uneven_subset(uneven_specs(), args.uneven_subset)
     b = cg.Batch(specs)
     rng = np.random.default_rng(5)
     host_in = torch.empty(b.in_bytes, dtype=torch.uint8).pin_memory()
@@ -458,7 +484,7 @@ def run_uneven(args):
     out = d_out.cpu().numpy()
     import oracle  # noqa: F401
 
-    chk = np.random.default_rng(6).choice(len(specs), 200, replace=False)
+    chk = np.random.default_rng(6).choice(len(specs), min(200, len(specs)), replace=False)
     worst = 0.0
     for i in chk:
         kind, n, method, _ = specs[i]
@@ -504,6 +530,7 @@ def run_uneven(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uniform[-1,1))",
         "config": {"workload": "uneven batch: 10000 jobs, lengths log-uniform [16, 65536], 60% C2C (15% of all prime), "
                                "20% RFft1D, 10% DCT-II, 10% MDCT 2048 sine; one work-queue launch in a CUDA graph",
+                   "subset": args.uneven_subset,
                    "l2": "flushed between timed steps", "tasks": info.tasks, "ctas": info.ctas,
                    "four_step_lengths": info.four_step_lengths, "one_cta_lengths": info.one_cta_lengths},
         "hbm_gbs": round(nbytes / (ms * 1e-3) / 1e9, 1),
@@ -861,6 +888,8 @@ def main():
                     help="large workload: fused four-step settings to time (lead,ring,hints; ';'-separated)")
     ap.add_argument("--fused-batches", default="",
                     help="large workload: sub-batch sizes timed two-launch vs the first --fused setting")
+    ap.add_argument("--uneven-subset", default="all", choices=["all", "small", "big_c2c", "big_prime", "big_real"],
+                    help="uneven workload: time one class of its jobs (profiling)")
     ap.add_argument("--small", action="store_true",
                     help="large workload only: the same kernels at 1/4 and 1/2 the batch (profiling case)")
     ap.add_argument("--workload", choices=["batch", "large", "uneven", "costmodel", "f64"], default="batch",

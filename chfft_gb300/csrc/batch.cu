@@ -398,10 +398,13 @@ int chfft_batch_create(int dtype, const chfft_batch_job* jobs, size_t njobs, chf
         nctr += 4;
         for (int t = 0; t < na; t++) lv[0].push_back({BT_FS_A, (int)i, wa, hb.blue ? 1 : 0, t, -1, 0, c0});
         const int bmode = hb.blue ? 1 : (x.kind == BK_C2C ? 0 : 3);
-        for (int t = 0; t < nb; t++) lv[1].push_back({BT_FS_B, (int)i, wb, bmode, t, c0, na, c0 + 1});
+        // A task whose counter nobody waits for (the last step of a C2C
+        // item) skips the signal and its store fence.
+        const int b_sig = (hb.blue || x.kind != BK_C2C) ? c0 + 1 : -1;
+        for (int t = 0; t < nb; t++) lv[1].push_back({BT_FS_B, (int)i, wb, bmode, t, c0, na, b_sig});
         if (hb.blue) {
           for (int t = 0; t < na; t++) lv[2].push_back({BT_FS_A, (int)i, wa, 2, t, c0 + 1, nb, c0 + 2});
-          for (int t = 0; t < nb; t++) lv[3].push_back({BT_FS_B, (int)i, wb, 2, t, c0 + 2, na, c0 + 3});
+          for (int t = 0; t < nb; t++) lv[3].push_back({BT_FS_B, (int)i, wb, 2, t, c0 + 2, na, -1});
         }
         if (x.kind != BK_C2C) {
           const int pairs = (int)((x.n + 3) / 4);

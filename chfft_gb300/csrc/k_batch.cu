@@ -95,16 +95,14 @@ __device__ __forceinline__ void real_post(const BatchItem& it, char* out_base, i
 
 __device__ __forceinline__ void wait_for(const BatchArgs& A, int ctr, int target) {
   if (threadIdx.x == 0) {
-    volatile int* c = A.ctr + ctr;
     int it = 0;
-    while (*c < target) {
+    while (ld_acquire(A.ctr + ctr) < target) {  // acquire: the producers' stores are visible after it
       if (++it > A.spin_limit) {
         atomicExch(A.err, 1);
         break;
       }
       __nanosleep(200);
     }
-    __threadfence();
   }
   __syncthreads();
 }

@@ -352,12 +352,6 @@ __global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_rows_t(c
   rows_t_tile<T, CoreT, MODE, false>(a, fs, tr, tr, r0, smem_raw);
 }
 
-__device__ __forceinline__ int ld_acquire(const int* p) {
-  int v;
-  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-
 // Both passes of a plain four-step batch in one launch of one CTA per tile.
 // A CTA takes its task from a ticket counter once it runs, so it only ever
 // waits on tasks that running CTAs hold (no deadlock whatever the residency).

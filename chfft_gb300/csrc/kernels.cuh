@@ -107,6 +107,13 @@ __device__ __forceinline__ double2 ld_policy(const double2* p, unsigned long lon
   asm volatile("ld.global.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(v.x), "=d"(v.y) : "l"(p), "l"(pol));
   return v;
 }
+// GPU-scope acquire load of a dependency counter.
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
 // L2-only loads (no L1 allocation) with an eviction priority.
 __device__ __forceinline__ float2 ld_cg_policy(const float2* p, unsigned long long pol) {
   float2 v;
