@@ -5,8 +5,9 @@
 // The host side groups the jobs by (kind, length, option), builds each
 // distinct length's tables once (FP64-generated, like every plan), decides
 // per length between a one-CTA task and a four-step task chain, and writes
-// the task queue: four-step levels first (column tiles, row tiles, Bluestein
-// second FFT, real-kind post tasks), then the one-CTA tasks by decreasing
+// the task queue: four-step levels first (column tiles; row tiles, which
+// for Bluestein also run the spectrum product and the inverse FFT's first
+// pass; the inverse's last pass; real-kind post tasks), then the one-CTA tasks by decreasing
 // cost. The queue and every table live in device memory; a launch only
 // passes the input / output base pointers, so it can be captured once and
 // replayed.
@@ -397,14 +398,18 @@ int chfft_batch_create(int dtype, const chfft_batch_job* jobs, size_t njobs, chf
         const int c0 = nctr;
         nctr += 4;
         for (int t = 0; t < na; t++) lv[0].push_back({BT_FS_A, (int)i, wa, hb.blue ? 1 : 0, t, -1, 0, c0});
-        const int bmode = hb.blue ? 1 : (x.kind == BK_C2C ? 0 : 3);
-        // A task whose counter nobody waits for (the last step of a C2C
-        // item) skips the signal and its store fence.
-        const int b_sig = (hb.blue || x.kind != BK_C2C) ? c0 + 1 : -1;
-        for (int t = 0; t < nb; t++) lv[1].push_back({BT_FS_B, (int)i, wb, bmode, t, c0, na, b_sig});
         if (hb.blue) {
-          for (int t = 0; t < na; t++) lv[2].push_back({BT_FS_A, (int)i, wa, 2, t, c0 + 1, nb, c0 + 2});
-          for (int t = 0; t < nb; t++) lv[3].push_back({BT_FS_B, (int)i, wb, 2, t, c0 + 2, na, -1});
+          // Forward rows + spectrum + the inverse's rows (FS_BB), then the
+          // inverse's n1-long rows with the chirp-out (FS_C).
+          const int wc = fs_width(hb.ca.d.st), nc = (hb.fs.n2 + wc - 1) / wc;
+          for (int t = 0; t < nb; t++) lv[1].push_back({BT_FS_BB, (int)i, wb, 0, t, c0, na, c0 + 1});
+          for (int t = 0; t < nc; t++) lv[2].push_back({BT_FS_C, (int)i, wc, 0, t, c0 + 1, nb, -1});
+        } else {
+          const int bmode = x.kind == BK_C2C ? 0 : 3;
+          // A task whose counter nobody waits for (the last step of a C2C
+          // item) skips the signal and its store fence.
+          const int b_sig = x.kind != BK_C2C ? c0 + 1 : -1;
+          for (int t = 0; t < nb; t++) lv[1].push_back({BT_FS_B, (int)i, wb, bmode, t, c0, na, b_sig});
         }
         if (x.kind != BK_C2C) {
           const int pairs = (int)((x.n + 3) / 4);
@@ -445,8 +450,8 @@ int chfft_batch_create(int dtype, const chfft_batch_job* jobs, size_t njobs, chf
       const BatchItem& it = items[t.item];
       size_t need = 0;
       if (t.type == BT_SMALL) need = (size_t)t.count * smem_ld(it.core.st.n) * 8;
-      else if (t.type == BT_FS_A) need = (size_t)t.count * smem_ld(it.ca.st.n) * 8;
-      else if (t.type == BT_FS_B) need = (size_t)t.count * smem_ld(it.cb.st.n) * 8;
+      else if (t.type == BT_FS_A || t.type == BT_FS_C) need = (size_t)t.count * smem_ld(it.ca.st.n) * 8;
+      else if (t.type == BT_FS_B || t.type == BT_FS_BB) need = (size_t)t.count * smem_ld(it.cb.st.n) * 8;
       smem = std::max(smem, need);
     }
     // ---- upload

@@ -139,7 +139,7 @@ __device__ __forceinline__ void batch_task(const BatchArgs& A, int ti, unsigned 
   }
 
   // ---- the core and its tile
-  const BatchCore& core = tk.type == BT_SMALL ? it.core : (tk.type == BT_FS_A ? it.ca : it.cb);
+  const BatchCore& core = tk.type == BT_SMALL ? it.core : (tk.type == BT_FS_A || tk.type == BT_FS_C ? it.ca : it.cb);
   const int m = core.st.n;
   // SMALL: transforms in the task; FS_A / FS_B: tile width (a power of two).
   const int tpb = tk.count;
@@ -183,29 +183,49 @@ __device__ __forceinline__ void batch_task(const BatchArgs& A, int ti, unsigned 
       }
       sm.store(t, i, v);
     }
-  } else {  // BT_FS_B
+  } else {  // BT_FS_B / BT_FS_BB: rows of n2 of the workspace; BT_FS_C: rows of n1 of the second workspace
     const int r0 = tk.tile * tpb;
-    const C* w = reinterpret_cast<const C*>(A.work + it.work_off);
+    const bool c = tk.type == BT_FS_C;
+    const C* w = reinterpret_cast<const C*>(A.work + (c ? it.work2_off : it.work_off));
+    const int nrows = c ? fs.n2 : fs.n1;
     for (int b = tid; b < tpb * m; b += nth) {
       const int t = b / m, i = b - t * m;  // consecutive threads along a row
       const int row = r0 + t;
-      sm.store(t, i, row < fs.n1 ? ldcg(w + (long long)row * fs.n2 + i) : czero<C>());
+      sm.store(t, i, row < nrows ? ldcg(w + (long long)row * m + i) : czero<C>());
     }
   }
   __syncthreads();
 
-  // ---- complex core (one call site for every task type)
+  // ---- complex core
+  // Between the two FFT rounds of a Bluestein core (one-CTA SMALL) or of an
+  // FS_BB row tile: the spectrum product, conjugated for the inverse.
+  auto between = [&]() {
+    if (core.blue) {
+      spectrum_phase<false>(sm, m, tpb, static_cast<const C*>(core.bhat));
+      return;
+    }
+    // conj(X_k B^_k) at natural index k = k1 + n1 k2 (row k1, element k2)
+    const int r0 = tk.tile * tpb;
+    const C* bh = static_cast<const C*>(fs.bhat);
+    for (int b = tid; b < tpb * m; b += nth) {
+      const int t = b / m, k2 = b - t * m;
+      const int k1 = min(r0 + t, fs.n1 - 1);  // rows past n1 are never stored
+      sm.store(t, k2, cconj(cmul(sm.load(t, k2), __ldg(&bh[k1 + (long long)fs.n1 * k2]))));
+    }
+    __syncthreads();
+  };
+  const bool two_rounds = core.blue || tk.type == BT_FS_BB;
   if constexpr (PERSIST) {  // one call site inside the task loop
-    for (int r = 0; r < (core.blue ? 2 : 1); r++) {
-      if (r == 1) spectrum_phase<false>(sm, m, tpb, static_cast<const C*>(core.bhat));
+    for (int r = 0; r < (two_rounds ? 2 : 1); r++) {
+      if (r == 1) between();
       smem_passes<false, false, kBatchEpt>(core.st.all, m, 1, tpb, static_cast<const C*>(core.tw), sm);
     }
   } else {
-    // Two call sites rather than a loop over the Bluestein rounds: a loop
-    // around the passes makes the compiler spill.
+    // Two call sites rather than a loop over the rounds: a loop around the
+    // passes makes the compiler spill.
     smem_passes<false, false, kBatchEpt>(core.st.all, m, 1, tpb, static_cast<const C*>(core.tw), sm);
-    if (core.blue) {
-      spectrum_phase<false>(sm, m, tpb, static_cast<const C*>(core.bhat));
+    if (two_rounds) {
+      between();
       smem_passes<false, false, kBatchEpt>(core.st.all, m, 1, tpb, static_cast<const C*>(core.tw), sm);
     }
   }
@@ -253,6 +273,30 @@ __device__ __forceinline__ void batch_task(const BatchArgs& A, int ti, unsigned 
       const long long e = (long long)k1 * col;
       const C tw = cmul(__ldg(&hi[e >> fs.tw_shift]), __ldg(&lo[e & ((1LL << fs.tw_shift) - 1)]));
       w[(long long)k1 * fs.n2 + col] = cmul(sm.load(t, k1), tw);
+    }
+  } else if (tk.type == BT_FS_BB) {  // G[k1][m2] w_M^(k1 m2) -> second workspace [m2][k1]
+    const int r0 = tk.tile * tpb;
+    C* w2 = reinterpret_cast<C*>(A.work + it.work2_off);
+    const C* lo = static_cast<const C*>(fs.lo);
+    const C* hi = static_cast<const C*>(fs.hi);
+    for (int b = tid; b < tpb * m; b += nth) {
+      const int t = b & (tpb - 1), m2 = b >> lw;  // consecutive threads: adjacent k1
+      const int k1 = r0 + t;
+      if (k1 >= fs.n1) continue;
+      const long long e = (long long)k1 * m2;
+      const C tw = cmul(__ldg(&hi[e >> fs.tw_shift]), __ldg(&lo[e & ((1LL << fs.tw_shift) - 1)]));
+      w2[k1 + (long long)fs.n1 * m2] = cmul(sm.load(t, m2), tw);
+    }
+  } else if (tk.type == BT_FS_C) {  // F[m2 + n2 m1]: conj(F) c_m, m < n_user
+    const int r0 = tk.tile * tpb;
+    C* o = reinterpret_cast<C*>(A.out + it.out_off);
+    const C* ch = static_cast<const C*>(fs.chirp);
+    for (int b = tid; b < tpb * m; b += nth) {
+      const int t = b & (tpb - 1), m1 = b >> lw;  // consecutive threads: adjacent m2
+      const int m2 = r0 + t;
+      if (m2 >= fs.n2) continue;
+      const long long k = m2 + (long long)fs.n2 * m1;
+      if (k < fs.n_user) o[k] = cmul(cconj(sm.load(t, m1)), __ldg(&ch[k]));
     }
   } else {  // BT_FS_B: X[k1 + n1 k2]
     const int r0 = tk.tile * tpb;

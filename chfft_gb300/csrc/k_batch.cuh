@@ -11,6 +11,14 @@
 //          Bluestein spectrum, Bluestein chirp-out, or the core output of a
 //          real kind for its POST tasks)
 //   POST   the R2C split / DCT-II post-twiddle of a four-step real kind
+//   FS_BB  four-step Bluestein middle: a row tile's forward FFT (n2), the
+//          spectrum product, the row FFT of the inverse transform (n2) and
+//          its twiddle, stored transposed (the inverse's row-major n2 x n1)
+//   FS_C   four-step Bluestein last: row FFTs of length n1 of that
+//          intermediate, chirp-out store in natural order
+// A four-step Bluestein item runs FS_A (chirp in), FS_BB, FS_C: the
+// inverse FFT is split with the roles of n1 and n2 swapped, so its first
+// pass works on the rows the forward FFT's last pass already holds.
 // Dependencies are device counters: a task waits (bounded spin, thread 0)
 // until its counter reaches the number of tiles of the step it consumes,
 // and signals its own counter when done. Tasks are queued level by level, so
@@ -28,7 +36,7 @@ constexpr int kBatchTile = 16;     // narrowest four-step tile (columns / rows)
 constexpr int kBatchTileMax = 64;  // widest four-step tile
 
 enum BatchKind : int { BK_C2C = 0, BK_R2C = 1, BK_DCT2 = 2, BK_MDCT = 3 };
-enum BatchTaskType : int { BT_SMALL = 0, BT_FS_A = 1, BT_FS_B = 2, BT_POST = 3 };
+enum BatchTaskType : int { BT_SMALL = 0, BT_FS_A = 1, BT_FS_B = 2, BT_POST = 3, BT_FS_BB = 4, BT_FS_C = 5 };
 
 struct BatchCore {
   StageList st;       // stages run (length M for Bluestein)
