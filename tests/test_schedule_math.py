@@ -1,0 +1,93 @@
+"""CPU: the index algebra and task orders the kernels rely on, restated in
+numpy / Python and checked on small cases (the GPU tests check the kernels).
+
+- three-pass four-step Bluestein of the uneven batch (k_batch.cu FS_A,
+  FS_BB, FS_C): forward FFT with k = k1 + n1 k2, spectrum product, inverse
+  FFT split as m = m2 + n2 m1 so its first pass runs over the same rows;
+- the fused four-step launch's ticket order (k_complex.cuh
+  k_fourstep_fused): every tile appears once, and every wait is on tickets
+  taken earlier, for any batch, lead and ring.
+"""
+import numpy as np
+import pytest
+
+
+def chirp(n):
+    j = np.arange(n)
+    # exp(-i pi j^2 / n) with j^2 reduced mod 2n exactly in integers
+    return np.exp(-1j * np.pi * ((j * j) % (2 * n)) / n)
+
+
+def bluestein_three_pass(x, n1, n2):
+    n = x.size
+    M = n1 * n2
+    c = chirp(n)
+    # B^ = FFT_M(conj c, wrapped) / M
+    b = np.zeros(M, complex)
+    b[:n] = np.conj(c)
+    b[M - n + 1:] = np.conj(c[1:])[::-1]
+    bhat = np.fft.fft(b) / M
+    a = np.zeros(M, complex)
+    a[:n] = x * c
+    # FS_A: column FFTs of length n1 over j1 (x[j1 n2 + j2]), twiddle w_M^(k1 j2)
+    A = a.reshape(n1, n2)
+    Y = np.fft.fft(A, axis=0) * np.exp(-2j * np.pi * np.outer(np.arange(n1), np.arange(n2)) / M)
+    # FS_BB: per row k1: FFT over j2 -> Z[k1][k2] (X at k = k1 + n1 k2), spectrum, conj,
+    # FFT over k2 -> G[k1][m2], twiddle w_M^(k1 m2), stored as [m2][k1]
+    Z = np.fft.fft(Y, axis=1)
+    k = np.arange(n1)[:, None] + n1 * np.arange(n2)[None, :]
+    V = np.conj(Z * bhat[k])
+    G = np.fft.fft(V, axis=1) * np.exp(-2j * np.pi * np.outer(np.arange(n1), np.arange(n2)) / M)
+    W = G.T  # rows m2, n1 long
+    # FS_C: FFT over k1 per row m2 -> F[m2 + n2 m1]; out = conj(F) c for m < n
+    F = np.fft.fft(W, axis=1)
+    m = np.arange(n2)[:, None] + n2 * np.arange(n1)[None, :]
+    out = np.zeros(M, complex)
+    out[m.ravel()] = F.ravel()
+    return np.conj(out[:n]) * c
+
+
+@pytest.mark.parametrize("n,n1,n2", [(17, 5, 8), (101, 16, 14), (1009, 45, 48), (10007, 140, 144)])
+def test_three_pass_bluestein_matches_dft(n, n1, n2):
+    assert n1 * n2 >= 2 * n - 1
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    got = bluestein_three_pass(x, n1, n2)
+    ref = np.fft.fft(x)
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-12
+
+
+def decode(t, count, ta, tb, lead):
+    """Ticket t -> (is_a, transform, tile), as k_fourstep_fused decodes it."""
+    per, pairs = ta + tb, count - lead
+    if t < lead * ta:
+        k = t // ta
+        return True, k, t - k * ta
+    if t - lead * ta < pairs * per:
+        u = t - lead * ta
+        j, r = divmod(u, per)
+        return (True, j + lead, r) if r < ta else (False, j, r - ta)
+    v = t - lead * ta - pairs * per
+    k = pairs + v // tb
+    return False, k, v - (k - pairs) * tb
+
+
+@pytest.mark.parametrize("count", [1, 2, 3, 5, 9])
+@pytest.mark.parametrize("ta,tb", [(1, 1), (3, 2), (4, 7)])
+@pytest.mark.parametrize("lead,ring", [(1, 2), (2, 3), (2, 4), (3, 5), (4, 4)])
+def test_fused_ticket_order(count, ta, tb, lead, ring):
+    # the host clamps as plan.cu does
+    lead = min(lead, count)
+    ring = min(max(ring, lead + 1), count)
+    pos = {}
+    for t in range(count * (ta + tb)):
+        is_a, k, tile = decode(t, count, ta, tb, lead)
+        assert 0 <= k < count and 0 <= tile < (ta if is_a else tb)
+        assert (is_a, k, tile) not in pos
+        pos[(is_a, k, tile)] = t
+    assert len(pos) == count * (ta + tb)
+    for (is_a, k, _), t in pos.items():
+        if is_a and k >= ring:  # waits for every B(k - ring) tile: its ring slot is free
+            assert all(pos[(False, k - ring, x)] < t for x in range(tb))
+        if not is_a:  # waits for every A(k) tile
+            assert all(pos[(True, k, x)] < t for x in range(ta))
