@@ -122,6 +122,7 @@ const char* kernel_template(Kernel k) {
     case Kernel::IMDCT: return "chfft::kern::k_imdct";
     case Kernel::COLS_TW: return "chfft::kern::k_cols_tw";
     case Kernel::ROWS_T: return "chfft::kern::k_rows_t";
+    case Kernel::ROWS_BB: return "chfft::kern::k_rows_bb";
   }
   return "";
 }
@@ -133,8 +134,10 @@ int pad_period(const StageList& st) {
   return (!order.empty() && order[0] % 2 == 0) ? order[0] : 0;
 }
 
-bool column_mapped(Kernel k) { return k == Kernel::COLS || k == Kernel::COLS_TW || k == Kernel::ROWS_T; }
-bool four_step(Kernel k) { return k == Kernel::COLS_TW || k == Kernel::ROWS_T; }
+bool column_mapped(Kernel k) {
+  return k == Kernel::COLS || k == Kernel::COLS_TW || k == Kernel::ROWS_T || k == Kernel::ROWS_BB;
+}
+bool four_step(Kernel k) { return k == Kernel::COLS_TW || k == Kernel::ROWS_T || k == Kernel::ROWS_BB; }
 
 // Tile stride of a specialised kernel. Column-mapped passes give the lanes
 // of one shared-memory wavefront (16 f32 / 8 f64 complex elements) tpb

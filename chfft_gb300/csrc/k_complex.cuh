@@ -352,6 +352,73 @@ __global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_rows_t(c
   rows_t_tile<T, CoreT, MODE, false>(a, fs, tr, tr, r0, smem_raw);
 }
 
+// ---------------------------------------------------------------- four-step Bluestein
+// Middle pass of a four-step Bluestein transform (three passes instead of
+// four). Rows k1 of pass A's output (n2 long): their FFT gives X at the
+// natural index k = k1 + n1 k2; the inverse transform's input is
+// conj(X_k B^_k) (the conjugation trick). The inverse FFT of length
+// M = n1 n2 is split the other way round, m = m2 + n2 m1, so its first pass
+// is again an n2-point FFT over k2 of the same row, followed by the twiddle
+// w_M^(k1 m2); the row tile therefore runs two FFTs back to back and stores
+// the intermediate as the n2 x n1 matrix [m2][k1] (contiguous runs of
+// adjacent k1). The last pass is k_rows_t's chirp-out mode over the rows of
+// that matrix (n1 and n2 swapped in its FourStep).
+template <typename C, class Tile>
+struct RowSpectrumStore {
+  const Tile& sm;
+  const C* bhat;
+  int r0, n1;
+  __device__ __forceinline__ void store(int t, int k2, C v) const {
+    const int k1 = min(r0 + t, n1 - 1);  // rows past n1 are never stored
+    sm.store(t, k2, cconj(cmul(v, __ldg(&bhat[k1 + (long long)n1 * k2]))));
+  }
+};
+
+template <typename C, bool HINTS>
+struct RowsBBStore {
+  C* out;  // the transform's n2 x n1 intermediate
+  int r0, nvalid, n1;
+  const FourStep* fs;
+  unsigned long long pol;
+  __device__ __forceinline__ void store(int t, int m2, C v) const {
+    if (t >= nvalid) return;
+    const int k1 = r0 + t;
+    const long long e = (long long)k1 * m2;  // < M
+    const C* lo = static_cast<const C*>(fs->lo);
+    const C* hi = static_cast<const C*>(fs->hi);
+    const C w = cmul(__ldg(&hi[e >> fs->tw_shift]), __ldg(&lo[e & ((1LL << fs->tw_shift) - 1)]));
+    const long long k = k1 + (long long)n1 * m2;
+    if constexpr (HINTS)
+      st_policy(out + k, cmul(v, w), pol);
+    else
+      out[k] = cmul(v, w);
+  }
+};
+
+template <typename T, class CoreT, int MODE>
+__global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_rows_bb(const KArgs a, const FourStep fs) {
+  using C = cx_t<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
+  const long long tr = blockIdx.x / a.tiles_per_tr;
+  const int r0 = (int)(blockIdx.x - tr * a.tiles_per_tr) * a.tpb;
+  const int nvalid = min(a.tpb, fs.n1 - r0);
+  constexpr bool kHints = (MODE & kL2Hints) != 0;
+  const unsigned long long pin = kHints ? l2_evict_first() : 0ull;
+  const unsigned long long pout = kHints ? l2_evict_last() : 0ull;
+  RowsBLoad<C, kHints> rl{(const C*)a.in + tr * a.in_dist + (long long)r0 * fs.n2, fs.n2, nvalid, pin};
+  RowSpectrumStore<C, decltype(sm)> spec{sm, static_cast<const C*>(fs.bhat), r0, fs.n1};
+  RowsBBStore<C, kHints> st{(C*)a.out + tr * a.out_dist, r0, nvalid, fs.n1, &fs, pout};
+  if constexpr (CoreT::kStatic) {
+    CoreT::template run<true>(a.core, a.tpb, sm, rl, spec);
+    CoreT::template run<false>(a.core, a.tpb, sm, sm, st);
+  } else {
+    load_phase<false>(sm, fs.n2, a.tpb, rl);
+    CoreT::run(a.core, a.tpb, sm, sm, spec);
+    CoreT::run(a.core, a.tpb, sm, sm, st);
+  }
+}
+
 // Both passes of a plain four-step batch in one launch of one CTA per tile.
 // A CTA takes its task from a ticket counter once it runs, so it only ever
 // waits on tasks that running CTAs hold (no deadlock whatever the residency).
@@ -445,7 +512,8 @@ cudaError_t launch_fourstep(bool pass_a, int mode, bool k1, const KArgs& a, cons
     using KNC = DynCore<false, true, true, false>;
     if (mode == 0) fn = k1 ? k_rows_t<T, K1C, 0> : k_rows_t<T, KNC, 0>;
     else if (mode == 1) fn = k1 ? k_rows_t<T, K1C, 1> : k_rows_t<T, KNC, 1>;
-    else fn = k1 ? k_rows_t<T, K1C, 2> : k_rows_t<T, KNC, 2>;
+    else if (mode == 2) fn = k1 ? k_rows_t<T, K1C, 2> : k_rows_t<T, KNC, 2>;
+    else fn = k1 ? k_rows_bb<T, K1C, 0> : k_rows_bb<T, KNC, 0>;  // 3: Bluestein middle pass
   }
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

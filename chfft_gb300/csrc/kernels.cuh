@@ -60,6 +60,7 @@ enum class Kernel : int {
   IMDCT = 7,
   COLS_TW = 8,  // four-step pass A
   ROWS_T = 9,   // four-step pass B
+  ROWS_BB = 10, // four-step Bluestein middle pass (k_rows_bb)
 };
 
 // Four-step geometry of a length-N FFT beyond one CTA, N = n1 * n2.
@@ -134,7 +135,8 @@ __device__ __forceinline__ void st_policy(double2* p, double2 v, unsigned long l
 
 #ifndef __CUDACC_RTC__
 // Four-step passes: pass_a selects the column pass (mode 0 plain, 1 chirp
-// input) or the transposing row pass (mode 0 plain, 1 spectrum, 2 chirp output).
+// input) or the transposing row pass (mode 0 plain, 1 spectrum, 2 chirp
+// output, 3 the Bluestein middle pass k_rows_bb).
 template <typename T>
 cudaError_t launch_fourstep(bool pass_a, int mode, bool k1, const KArgs& a, const FourStep& fs, unsigned blocks,
                             unsigned threads, size_t smem, cudaStream_t stream);

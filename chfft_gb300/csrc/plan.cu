@@ -9,6 +9,7 @@
 #include "plan.hpp"
 
 #include <algorithm>
+#include <utility>
 #include <climits>
 #include <cmath>
 #include <cstdio>
@@ -398,8 +399,8 @@ static void launch_pass(bool pass_a, int mode, const Core& c, const Geo& g, cons
     if (r == 1) throw Fail{CHFFT_EUNSUPPORTED, "tensor-core kernel unavailable (plan compiler or geometry)"};
     return;
   }
-  if (!library_only && want_specialised(elems, jit_opt) &&
-      jit_launch(pass_a ? Kernel::COLS_TW : Kernel::ROWS_T, c.dtype, c, g, a, blocks, s, jmode, &fs) == 0)
+  const Kernel kk = pass_a ? Kernel::COLS_TW : (mode == 3 ? Kernel::ROWS_BB : Kernel::ROWS_T);
+  if (!library_only && want_specialised(elems, jit_opt) && jit_launch(kk, c.dtype, c, g, a, blocks, s, jmode, &fs) == 0)
     return;
   CHFFT_CUDA(c.dtype == 0 ? launch_fourstep<float>(pass_a, mode, g.k1, a, fs, blocks, g.threads, g.smem, s)
                           : launch_fourstep<double>(pass_a, mode, g.k1, a, fs, blocks, g.threads, g.smem, s));
@@ -623,6 +624,28 @@ void BigCore::exec(const void* in, void* out, void* work, long long batch, bool 
     if (!blue) {
       pass_a(0, src, n, tmp, scale, back);
       pass_b(0, tmp, dst, n, back);
+    } else if (tc <= 0) {
+      // Three passes: the inverse FFT is split m = m2 + n2 m1, so its first
+      // pass (n2-point FFTs over k2) runs in the forward row pass's CTAs.
+      pass_a(1, src, n, tmp, scale, back);  // x c, zero padded
+      pass_b(3, tmp, tmp2, m, 0);           // FFT_n2, conj(X B^), FFT_n2, w_M^(k1 m2) -> [m2][k1]
+      FourStep fw = f;                      // the last pass sees the n2 x n1 intermediate
+      std::swap(fw.n1, fw.n2);
+      Geo gc = col_geo(ca, n2, tile_default, opts);
+      KArgs a{};
+      a.core = ca.desc();
+      a.tpb = gc.tpb;
+      a.ld = gc.ld;
+      a.back = back;
+      a.count = cnt;
+      a.tiles_per_tr = (n2 + gc.tpb - 1) / gc.tpb;
+      a.in = tmp2;
+      a.out = dst;
+      a.scale = 1.0;
+      a.in_dist = m;
+      a.out_dist = n;
+      a.ncols = n1;
+      launch_pass(false, 2, ca, gc, a, fw, (unsigned)(cnt * a.tiles_per_tr), cnt * m, s, library_only, opts.jit, tc);
     } else {
       pass_a(1, src, n, tmp, scale, back);  // x c, zero padded
       pass_b(1, tmp, tmp2, m, 0);           // conj(X B^)
