@@ -634,10 +634,9 @@ def run_large(args):
                           "speedup_vs_fp32": round(part_ms[i] / ms, 3)}
         tuning.set_config(plans[i], tuning.default_config())
         tc_parts[name] = row
-    # Four-step parts as one fused launch (both passes, ring of L2-resident
-    # intermediates, CHFFT_FUSED="lead,ring,hints"); output must equal the
-    # two-launch output bit for bit.
-    fused = {}
+    # Four-step parts: the pipelined launch (default) against the two-launch
+    # path (CHFFT_PIPE=0), and the pipelined launch's schedules (--pipe).
+    forms = {}
     for i, (name, n, batch) in enumerate(parts):
         if plans[i].info().algorithm != 2:
             continue
@@ -645,36 +644,20 @@ def run_large(args):
         fn()
         torch.cuda.synchronize()
         ref_out = d_out[i].clone()
-        row = {}
-        for spec in args.fused.split(";"):
-            os.environ["CHFFT_FUSED"] = spec
+        row = {"default_ms": round(part_ms[i], 4)}
+        for spec in ["0"] + [v for v in args.pipe.split(";") if v]:
+            os.environ["CHFFT_PIPE"] = spec
             try:
                 d_out[i].zero_()
                 fn()
                 torch.cuda.synchronize()
-                same = bool(torch.equal(d_out[i], ref_out))
+                diff = float((d_out[i] - ref_out).abs().max())
                 ms = time_events(fn, args.steps, args.warmup, None, stream)
-                row[spec] = {"ms": round(ms, 4), "bit_equal_two_launch": same,
-                             "speedup_vs_two_launch": round(part_ms[i] / ms, 3)}
+                row["two_launch" if spec == "0" else spec] = {"ms": round(ms, 4), "max_abs_diff_vs_default": diff,
+                                                                "default_speedup": round(ms / part_ms[i], 3)}
             finally:
-                os.environ.pop("CHFFT_FUSED", None)
-        # Sub-batches of the same plan and buffers: two-launch against the
-        # first setting, by batch size.
-        by_batch = {}
-        for sb in (int(v) for v in args.fused_batches.split(",") if v):
-            if sb > batch:
-                continue
-            fb = lambda: plans[i].execute_device("forward", d_in[i].data_ptr(), d_out[i].data_ptr(), sb, sptr)  # noqa: E731
-            two = time_events(fb, args.steps, args.warmup, None, stream)
-            os.environ["CHFFT_FUSED"] = args.fused.split(";")[0]
-            try:
-                one = time_events(fb, args.steps, args.warmup, None, stream)
-            finally:
-                os.environ.pop("CHFFT_FUSED", None)
-            by_batch[str(sb)] = {"two_launch_ms": round(two, 4), "fused_ms": round(one, 4),
-                                 "speedup": round(two / one, 3)}
-        row["by_batch"] = by_batch
-        fused[name] = row
+                os.environ.pop("CHFFT_PIPE", None)
+        forms[name] = row
         del ref_out
     e2e_t = []
     for i, (name, n, batch) in enumerate(parts):
@@ -704,7 +687,7 @@ def run_large(args):
                   for (name, n, b), t in zip(parts, part_ms)},
         "max_rel_l2_vs_fp64": worst,
         "tensor_core_form": tc_parts,
-        "fused_four_step": fused,
+        "four_step_forms": forms,
         "e2e": {"value": round(flops / e2e_s / 1e9, 2), "unit": "GFLOP/s",
                 "h2d_bytes_per_step": int(nbytes / 2), "d2h_bytes_per_step": int(nbytes / 2),
                 "ms_per_step": round(e2e_s * 1e3, 3)},
@@ -884,10 +867,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--fused", default="1,2,1;2,3,1;2,4,1;3,5,1;2,4,0",
-                    help="large workload: fused four-step settings to time (lead,ring,hints; ';'-separated)")
-    ap.add_argument("--fused-batches", default="",
-                    help="large workload: sub-batch sizes timed two-launch vs the first --fused setting")
+    ap.add_argument("--pipe", default="2,4,1;4,8,1;3,6,0",
+                    help="large workload: pipelined four-step schedules to time (lead,ring,hints; ';'-separated)")
     ap.add_argument("--uneven-subset", default="all", choices=["all", "small", "big_c2c", "big_prime", "big_real"],
                     help="uneven workload: time one class of its jobs (profiling)")
     ap.add_argument("--small", action="store_true",

@@ -90,6 +90,7 @@ def lib() -> ctypes.CDLL:
         "chfft_execute_2d": [vp, i, vp, sz, sz, vp],
         "chfft_execute_batch": [vp, i, vp, vp, sz],
         "chfft_execute_device": [vp, i, vp, vp, sz, vp],
+        "chfft_plan_wait": [vp, vp],
         "chfft_plan_get_info": [vp, ctypes.POINTER(PlanInfo)],
         "chfft_factorize": [sz, sz, vp, vp, sz],
         "chfft_digit_reversal": [vp, vp, sz, vp, sz],
@@ -206,6 +207,11 @@ class _Plan:
         """`batch` transforms on device pointers, enqueued on a CUDA stream handle."""
         _check(lib().chfft_execute_device(self._h, METHODS[method], ctypes.c_void_p(d_src), ctypes.c_void_p(d_dst),
                                           batch, ctypes.c_void_p(stream)))
+
+    def wait(self, stream: int = 0):
+        """Synchronise `stream`; raises (status ETIMEOUT) if a bounded device-side
+        wait of this plan's launches gave up since the last check."""
+        _check(lib().chfft_plan_wait(self._h, ctypes.c_void_p(stream)))
 
     def _sizes(self, back: bool):
         raise NotImplementedError

@@ -237,6 +237,16 @@ int chfft_execute_device(chfft_plan plan, int method, const void* d_src, void* d
   });
 }
 
+int chfft_plan_wait(chfft_plan plan, void* stream) {
+  if (!plan) return chfft::set_error(CHFFT_EINVAL, "null plan");
+  PlanImpl& p = plan->impl;
+  return guarded([&]() -> int {
+    CHFFT_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+    p.check_waits();
+    return (int)CHFFT_OK;
+  });
+}
+
 int chfft_plan_get_info(chfft_plan plan, chfft_plan_info* info) {
   if (!plan || !info) return chfft::set_error(CHFFT_EINVAL, "null argument");
   const PlanImpl& p = plan->impl;

@@ -356,34 +356,6 @@ int jit_launch(Kernel k, int dtype, const Core& c, const Geo& g0, const KArgs& a
   return 0;
 }
 
-int jit_launch_fused(const Core& ca, const Geo& ga0, const KArgs& a0, int mode_a, const Core& cb, const Geo& gb0,
-                     const KArgs& b0, int mode_b, const FourStep& fs, FusedSched f, cudaStream_t stream) {
-  if (ca.dtype != cb.dtype || ca.blue || cb.blue) return 1;
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (!load_api()) return 1;
-  Spec sa, sb;
-  if (!resolve(Kernel::COLS_TW, ca.dtype, ca, ga0, a0, mode_a, &fs, &sa) ||
-      !resolve(Kernel::ROWS_T, cb.dtype, cb, gb0, b0, mode_b, &fs, &sb))
-    return 1;
-  if (sa.g.threads != sb.g.threads) return 1;
-  const size_t smem = std::max(sa.g.smem, sb.g.smem);
-  std::string expr = "&chfft::kern::k_fourstep_fused<";
-  expr += ca.dtype == 0 ? "float, " : "double, ";
-  expr += core_expression(Kernel::COLS_TW, ca.dtype, ca, *sa.sl, sa.g) + ", ";
-  expr += core_expression(Kernel::ROWS_T, cb.dtype, cb, *sb.sl, sb.g) + ", ";
-  expr += std::to_string(mode_a) + ", " + std::to_string(mode_b) + ">";
-  CUfunction fn = nullptr;
-  if (int r = kernel_for(expr, smem, &fn)) return r;
-  const long long tasks = f.count * (f.tiles_a + (long long)f.tiles_b);
-  if (tasks > 0x7fffffffLL) return 1;
-  const unsigned blocks = (unsigned)tasks;
-  sa.a.ahead = sb.a.ahead = 0;
-  void* args[] = {&sa.a, &sb.a, const_cast<FourStep*>(&fs), &f};
-  if (g_api.cuLaunchKernel(fn, blocks, 1, 1, sa.g.threads, 1, 1, (unsigned)smem, (CUstream)stream, args, nullptr) != 0)
-    return 2;
-  return 0;
-}
-
 size_t tc_geometry(const Core& c, Kernel k, int tpb, int prec, int* ld_out) {
   if (c.dtype != 0 || c.blue || c.tc_s16 < 1 || !c.tcw.p || prec < 1 || prec > 3 || tpb < 1) return 0;
   const long long n = c.st.n;

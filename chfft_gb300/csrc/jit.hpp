@@ -18,13 +18,6 @@ bool jit_available(std::string* why);
 // caller launches the library kernel instead), 2 on a launch error.
 int jit_launch(Kernel k, int dtype, const Core& c, const Geo& g, const KArgs& a, unsigned blocks, cudaStream_t stream,
                int mode = 0, const FourStep* fs = nullptr);
-// Both four-step passes of a plain (non-Bluestein) batch in one launch of
-// one CTA per tile, k_fourstep_fused (k_complex.cuh), with the specialised cores of
-// jit_launch for (ca, ga, mode_a) and (cb, gb, mode_b); f.next / done_a /
-// done_b must be zero. Same return codes; 1 also when the two passes need
-// different CTA shapes.
-int jit_launch_fused(const Core& ca, const Geo& ga, const KArgs& a, int mode_a, const Core& cb, const Geo& gb,
-                     const KArgs& b, int mode_b, const FourStep& fs, FusedSched f, cudaStream_t stream);
 // Tensor-core variant: the kernel over a TcCore (radix-16 passes on the
 // tensor cores at precision prec 1..3, tc.cuh / tc_core.cuh) for a core with
 // a tensor-core pass order, tpb sequences per CTA. Same return codes; 1 also

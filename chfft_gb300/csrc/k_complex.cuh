@@ -289,9 +289,7 @@ struct RowsBStore {
   }
 };
 
-// CG: the intermediate was written earlier in the same launch (fused
-// four-step): read it from L2, never from a possibly stale L1 line.
-template <typename C, bool HINTS, bool CG = false>
+template <typename C, bool HINTS>
 struct RowsBLoad {
   const C* in;  // first row of the tile
   int n2, nvalid;
@@ -299,10 +297,6 @@ struct RowsBLoad {
   __device__ __forceinline__ C load(int t, int i) const {
     if (t >= nvalid) return czero<C>();
     const long long k = (long long)t * n2 + i;
-    if constexpr (CG) {
-      if constexpr (HINTS) return ld_cg_policy(in + k, pol);
-      return __ldcg(in + k);
-    }
     if constexpr (HINTS) return ld_policy(in + k, pol);
     return in[k];
   }
@@ -310,7 +304,7 @@ struct RowsBLoad {
 
 // One pass-B tile: rows [r0, r0 + tpb) of slot tr_in of a.in, transposed
 // into transform tr_out of a.out.
-template <typename T, class CoreT, int MODE, bool CG>
+template <typename T, class CoreT, int MODE>
 __device__ __forceinline__ void rows_t_tile(const KArgs& a, const FourStep& fs, long long tr_in, long long tr_out,
                                             int r0, unsigned char* smem_raw) {
   using C = cx_t<T>;
@@ -324,7 +318,7 @@ __device__ __forceinline__ void rows_t_tile(const KArgs& a, const FourStep& fs, 
   constexpr bool kHints = (MODE & kL2Hints) != 0;
   const unsigned long long pin = kHints ? l2_evict_first() : 0ull;
   const unsigned long long pout = kHints ? ((MODE & 3) == 1 ? l2_evict_last() : l2_evict_first()) : 0ull;
-  RowsBLoad<C, kHints, CG> rl{(const C*)a.in + tr_in * a.in_dist + (long long)r0 * fs.n2, fs.n2, nvalid, pin};
+  RowsBLoad<C, kHints> rl{(const C*)a.in + tr_in * a.in_dist + (long long)r0 * fs.n2, fs.n2, nvalid, pin};
   RowsBStore<C, MODE & 3, kHints> st{(C*)a.out + tr_out * a.out_dist, r0, nvalid, fs.n1, a.back, &fs, pout};
   if constexpr (CoreT::kStatic) {
     CoreT::template run<true>(a.core, a.tpb, sm, rl, st);
@@ -349,7 +343,7 @@ __global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_rows_t(c
   }
   const long long tr = blockIdx.x / a.tiles_per_tr;
   const int r0 = (int)(blockIdx.x - tr * a.tiles_per_tr) * a.tpb;
-  rows_t_tile<T, CoreT, MODE, false>(a, fs, tr, tr, r0, smem_raw);
+  rows_t_tile<T, CoreT, MODE>(a, fs, tr, tr, r0, smem_raw);
 }
 
 // ---------------------------------------------------------------- four-step Bluestein
@@ -416,81 +410,6 @@ __global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_rows_bb(
     load_phase<false>(sm, fs.n2, a.tpb, rl);
     CoreT::run(a.core, a.tpb, sm, sm, spec);
     CoreT::run(a.core, a.tpb, sm, sm, st);
-  }
-}
-
-// Both passes of a plain four-step batch in one launch of one CTA per tile.
-// A CTA takes its task from a ticket counter once it runs, so it only ever
-// waits on tasks that running CTAs hold (no deadlock whatever the residency).
-// The intermediate of transform k lives in ring slot k % ring and is
-// consumed a few transforms later, while it is still in L2, so HBM sees each
-// transform read once and written once. Waits are bounded: a time-out sets
-// the error word and later CTAs return at once.
-template <typename T, class CoreA, class CoreB, int MODE_A, int MODE_B>
-__global__ void __launch_bounds__(CoreA::kThreads,
-                                  (CoreA::kMinBlocks < CoreB::kMinBlocks ? CoreA::kMinBlocks : CoreB::kMinBlocks))
-    k_fourstep_fused(const KArgs a, const KArgs b, const FourStep fs, const FusedSched f) {
-  static_assert(CoreA::kThreads == CoreB::kThreads, "both passes run on the same CTA shape");
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ long long s_task;
-  __shared__ int s_ok;
-  const long long ta = f.tiles_a, tb = f.tiles_b, per = ta + tb;
-  const long long pairs = f.count - f.lead;
-  if (threadIdx.x == 0) s_task = (long long)atomicAdd(f.next, 1ull);
-  __syncthreads();
-  const long long t = s_task;
-  bool is_a;
-  long long k, tile;
-  if (t < f.lead * ta) {
-    is_a = true;
-    k = t / ta;
-    tile = t - k * ta;
-  } else if (t - f.lead * ta < pairs * per) {
-    const long long u = t - f.lead * ta, j = u / per, r = u - j * per;
-    is_a = r < ta;
-    k = is_a ? j + f.lead : j;
-    tile = is_a ? r : r - ta;
-  } else {
-    const long long v = t - f.lead * ta - pairs * per;
-    is_a = false;
-    k = pairs + v / tb;
-    tile = v - (k - pairs) * tb;
-  }
-  if (threadIdx.x == 0) {
-    const int* w = is_a ? (k >= f.ring ? f.done_b + (k - f.ring) : nullptr) : f.done_a + k;
-    const int need = is_a ? f.tiles_b : f.tiles_a;
-    int ok = *(volatile int*)f.err == 0;
-    if (ok && w) {
-      for (long long it = 0; ld_acquire(w) < need; it++) {
-        if (it >= f.spin_limit || *(volatile int*)f.err) {
-          ok = 0;
-          break;
-        }
-        __nanosleep(256);
-      }
-      if (!ok) atomicExch(f.err, 3);
-    }
-    s_ok = ok;
-  }
-  __syncthreads();
-  if (!s_ok) return;
-  const long long slot = k % f.ring;
-  if (is_a)
-    cols_tw_tile<T, CoreA, MODE_A>(a, fs, k, slot, (int)tile * a.tpb, smem_raw);
-  else
-    rows_t_tile<T, CoreB, MODE_B, true>(b, fs, slot, k, (int)tile * b.tpb, smem_raw);
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    if (is_a) {
-      // Pass B reads what this tile wrote: make every store of the CTA
-      // (ordered before the barrier) visible first.
-      __threadfence();
-      atomicAdd(f.done_a + k, 1);
-    } else if (k + f.ring < f.count) {
-      // A(k + ring) only overwrites what this tile read, and every load has
-      // completed (its value was stored before the barrier): no fence.
-      atomicAdd(f.done_b + k, 1);
-    }
   }
 }
 

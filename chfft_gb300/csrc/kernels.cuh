@@ -33,22 +33,6 @@ struct KArgs {
   long long ahead;         // > 0: prefetch into L2 the input of the CTA this many blocks later
 };
 
-// Schedule of the fused four-step launch (k_fourstep_fused, one CTA per
-// tile, tasks taken from a ticket counter): pass-A tiles
-// of transform k write ring slot k % ring, pass-B tiles of k read it. Tasks
-// are handed out in the order A(0..lead-1), then A(k + lead), B(k) for
-// k = 0, 1, ...; B(k) waits for every A(k) tile and A(k) for every B(k - ring)
-// tile (ring > lead), both earlier in the order.
-struct FusedSched {
-  unsigned long long* next;  // task counter
-  int* done_a;               // per transform: finished pass-A tiles
-  int* done_b;               // per transform: finished pass-B tiles
-  int* err;                  // 3: a dependency wait timed out (later CTAs then return)
-  long long count;           // transforms
-  int tiles_a, tiles_b, lead, ring;
-  long long spin_limit;      // polls (about 0.25 us apart) before a wait gives up
-};
-
 enum class Kernel : int {
   C2C = 0,
   COLS = 1,
@@ -115,17 +99,6 @@ __device__ __forceinline__ int ld_acquire(const int* p) {
   return v;
 }
 
-// L2-only loads (no L1 allocation) with an eviction priority.
-__device__ __forceinline__ float2 ld_cg_policy(const float2* p, unsigned long long pol) {
-  float2 v;
-  asm volatile("ld.global.cg.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(p), "l"(pol));
-  return v;
-}
-__device__ __forceinline__ double2 ld_cg_policy(const double2* p, unsigned long long pol) {
-  double2 v;
-  asm volatile("ld.global.cg.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(v.x), "=d"(v.y) : "l"(p), "l"(pol));
-  return v;
-}
 __device__ __forceinline__ void st_policy(float2* p, float2 v, unsigned long long pol) {
   asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(p), "f"(v.x), "f"(v.y), "l"(pol) : "memory");
 }

@@ -17,6 +17,8 @@
 
 #include "../../include/chfft_gpu.h"
 #include "jit.hpp"
+#include "k_pipe.cuh"
+#include "pipe.hpp"
 
 namespace chfft {
 
@@ -24,6 +26,33 @@ void cuda_check(cudaError_t e, const char* what) {
   if (e == cudaSuccess) return;
   int code = (e == cudaErrorMemoryAllocation) ? 5 /*CHFFT_ENOMEM*/ : 4 /*CHFFT_ECUDA*/;
   throw Fail{code, std::string(what) + ": " + cudaGetErrorString(e)};
+}
+
+HostWord::~HostWord() {
+  if (host) cudaFreeHost(host);
+}
+
+void HostWord::ensure() {
+  if (host) return;
+  void* h = nullptr;
+  CHFFT_CUDA(cudaHostAlloc(&h, sizeof(int), cudaHostAllocMapped));
+  host = static_cast<int*>(h);
+  *host = 0;
+  void* d = nullptr;
+  cudaError_t e = cudaHostGetDevicePointer(&d, h, 0);
+  if (e != cudaSuccess) {
+    cudaFreeHost(h);
+    host = nullptr;
+    cuda_check(e, "cudaHostGetDevicePointer");
+  }
+  dev = static_cast<int*>(d);
+}
+
+int HostWord::take() {
+  if (!host) return 0;
+  const int v = *(volatile int*)host;
+  if (v) *(volatile int*)host = 0;
+  return v;
 }
 
 void DevBuf::release() {
@@ -362,6 +391,19 @@ Geo col_geo(const Core& c, int ncols, int tpb_opt, const PlanOpts& o) {
   return g;
 }
 
+long long spin_limit() {
+  if (const char* e = std::getenv("CHFFT_SPIN_LIMIT")) {
+    const long long v = std::atoll(e);
+    if (v > 0) return v;
+  }
+  return 4000000;
+}
+
+int stall_test() {
+  const char* e = std::getenv("CHFFT_TEST_STALL");
+  return (e && e[0] == '1') ? 1 : 0;
+}
+
 bool want_specialised(long long elems, int jit_opt) {
   if (jit_opt >= 0) return jit_opt == 1;
   const JitMode mode = jit_mode();
@@ -449,6 +491,27 @@ bool BigCore::build(long long n_, int dtype_, cudaStream_t s, const PlanOpts& o)
     split(m, &n1, &n2);
   }
   if (!ca.build(n1, dtype, s) || !cb.build(n2, dtype, s)) return false;
+  pipe = false;
+  pstw_a.release();
+  pstw_b.release();
+  ptw.release();
+  if (!blue && dtype == 0 && pipe_shape_ok(n1, n2)) {
+    // Stage twiddles of the pipelined kernel's pass order (n/32, 32).
+    for (int side = 0; side < 2; side++) {
+      const int len = side ? n2 : n1;
+      PassList pl{};
+      pl.npass = 2;
+      pl.r[0] = len / 32;
+      pl.r[1] = 32;
+      DevBuf& b = side ? pstw_b : pstw_a;
+      b.ensure((size_t)(len - 1) * cb_);
+      CHFFT_CUDA(gen_stage_table<float>(pl, b.p, s));
+    }
+    ptw.ensure(pipe_twiddle_elems(n1, n2) * cb_);
+    CHFFT_CUDA(pipe_twiddles(n1, n2, ptw.p, s));
+    err.ensure();
+    pipe = true;
+  }
   tw_shift = tw_shift_for(m);
   tw_l = 1 << tw_shift;
   const long long nhi = (m + tw_l - 1) / tw_l;
@@ -505,12 +568,73 @@ long long BigCore::chunk(long long batch) const {
   return std::max(1LL, std::min(batch, (budget_mb << 20) / per));
 }
 
-// Plus 64 KiB (f32) for the fused launch's counters.
-long long BigCore::work_elems(long long batch) const { return chunk(batch) * m * (blue ? 2 : 1) + 8192; }
+// Plus 64 KiB (f32) and one element per transform for the pipelined
+// launch's counters (ticket, error word, per-transform tile counts).
+long long BigCore::work_elems(long long batch) const {
+  long long data = chunk(batch) * m * (blue ? 2 : 1);
+  int ring = 0, lead = 0, hints = 0;
+  if (pipe_params(batch, &ring, &lead, &hints)) data = std::max(data, (long long)ring * m);
+  return data + 8192 + batch;
+}
+
+// CHFFT_PIPE: "0" turns the pipelined launch off; "lead,ring,hints" sets its
+// schedule (tiles of `lead` transforms' column pass run ahead of the row
+// pass, `ring` intermediates, L2 eviction priorities on / off).
+bool BigCore::pipe_params(long long batch, int* ring, int* lead, int* hints) const {
+  if (!pipe || opts.tc > 0 || batch <= 0) return false;
+  int l = 3, r = 6, h = 1;
+  if (const char* e = std::getenv("CHFFT_PIPE")) {
+    if (e[0] == '0' && e[1] == 0) return false;
+    std::sscanf(e, "%d,%d,%d", &l, &r, &h);
+  }
+  l = (int)std::max<long long>(1, std::min<long long>(l, batch));
+  r = std::max(r, l + 1);
+  r = (int)std::min<long long>(r, batch);
+  *ring = r;
+  *lead = l;
+  *hints = h;
+  return true;
+}
 
 void BigCore::exec(const void* in, void* out, void* work, long long batch, bool back, double scale,
                    cudaStream_t s, long long max_chunk, bool library_only) const {
   const size_t cb_ = cplx_bytes(dtype);
+  int ring = 0, lead = 0, hints = 0;
+  if (!library_only && pipe_params(batch, &ring, &lead, &hints)) {
+    // Both passes in one persistent launch (k_pipe.cuh): ring slots of
+    // intermediates, then the counters (ticket, error word, tile counts).
+    char* ctr = static_cast<char*>(work) + (size_t)ring * m * cb_;
+    const size_t ctr_bytes = 16 + 8 * (size_t)batch;
+    CHFFT_CUDA(cudaMemsetAsync(ctr, 0, ctr_bytes, s));
+    pipe::PipeArgs a{};
+    a.out = static_cast<float2*>(out);
+    a.ring = static_cast<float2*>(work);
+    a.tiles_tw = static_cast<const float2*>(ptw.p);
+    a.stw_a = static_cast<const float2*>(pstw_a.p);
+    a.stw_b = static_cast<const float2*>(pstw_b.p);
+    a.ticket = reinterpret_cast<unsigned long long*>(ctr);
+    a.err = reinterpret_cast<int*>(ctr + 8);
+    a.sticky = err.dev;
+    a.done_a = reinterpret_cast<int*>(ctr + 16);
+    a.done_b = a.done_a + batch;
+    a.count = batch;
+    a.spin_limit = spin_limit();
+    a.lead = lead;
+    a.ring_slots = ring;
+    a.back = back ? 1 : 0;
+    a.scale = (float)scale;
+    a.hints = hints;
+    a.stall = stall_test();
+    int ta = 0, tb = 0;
+    pipe_tiles(n1, n2, &ta, &tb);
+    const long long tasks = batch * (long long)(ta + tb);
+    const int grid = (int)std::min<long long>(num_sms(), tasks);
+    const int r = pipe_launch(n1, n2, in, a, grid, s);
+    if (r == 2) throw Fail{CHFFT_ECUDA, "launch of the pipelined four-step kernel failed"};
+    if (r == 0) return;
+    // r == 1: the input cannot be described by a tensor map (alignment); the
+    // two-launch path below runs instead.
+  }
   const long long g = max_chunk > 0 ? std::min(chunk(batch), max_chunk) : chunk(batch);
   char* tmp = static_cast<char*>(work);
   char* tmp2 = tmp + g * m * cb_;
@@ -530,60 +654,6 @@ void BigCore::exec(const void* in, void* out, void* work, long long batch, bool 
     gb.tpb = tile(cb, Kernel::ROWS_T);
     if (!ga.tpb || !gb.tpb)
       throw Fail{CHFFT_EUNSUPPORTED, "tensor-core passes need power-of-two four-step factors >= 16"};
-  }
-  // Both passes in one launch over a ring of L2-resident intermediates
-  // (plain f32 four-step, specialised kernels; CHFFT_FUSED="lead,ring,hints").
-  int lead = 0, ring = 0, hints = 1;
-  if (const char* e = std::getenv("CHFFT_FUSED")) std::sscanf(e, "%d,%d,%d", &lead, &ring, &hints);
-  if (lead > 0 && !blue && dtype == 0 && tc <= 0 && !library_only && max_chunk <= 0 &&
-      want_specialised(batch * m, opts.jit)) {
-    lead = (int)std::min<long long>(lead, batch);
-    ring = (int)std::min<long long>(std::max(ring, lead + 1), batch);
-    const size_t ctr_bytes = 16 + 8 * (size_t)batch;
-    if ((size_t)ring * m * cb_ + ctr_bytes <= (size_t)work_elems(batch) * cb_) {
-      char* ctr = tmp + (size_t)ring * m * cb_;
-      CHFFT_CUDA(cudaMemsetAsync(ctr, 0, ctr_bytes, s));
-      FusedSched fz{};
-      fz.next = reinterpret_cast<unsigned long long*>(ctr);
-      fz.err = reinterpret_cast<int*>(ctr + 8);
-      fz.done_a = reinterpret_cast<int*>(ctr + 16);
-      fz.done_b = fz.done_a + batch;
-      fz.count = batch;
-      fz.tiles_a = (n2 + ga.tpb - 1) / ga.tpb;
-      fz.tiles_b = (n1 + gb.tpb - 1) / gb.tpb;
-      fz.lead = lead;
-      fz.ring = ring;
-      fz.spin_limit = 4000000;  // ~1 s
-      KArgs a{}, b{};
-      a.core = ca.desc();
-      a.tpb = ga.tpb;
-      a.ld = ga.ld;
-      a.back = back;
-      a.count = batch;
-      a.tiles_per_tr = fz.tiles_a;
-      a.in = in;
-      a.out = tmp;
-      a.scale = scale;
-      a.in_dist = n;
-      a.out_dist = m;
-      a.ncols = n2;
-      b.core = cb.desc();
-      b.tpb = gb.tpb;
-      b.ld = gb.ld;
-      b.back = back;
-      b.count = batch;
-      b.tiles_per_tr = fz.tiles_b;
-      b.in = tmp;
-      b.out = out;
-      b.scale = 1.0;
-      b.in_dist = m;
-      b.out_dist = n;
-      b.ncols = n2;
-      const int hb = hints ? 4 : 0;
-      const int r = jit_launch_fused(ca, ga, a, hb | 8, cb, gb, b, hb, f, fz, s);
-      if (r == 2) throw Fail{CHFFT_ECUDA, "launch of the fused four-step kernel failed"};
-      if (r == 0) return;
-    }
   }
   for (long long c0 = 0; c0 < batch; c0 += g) {
     const long long cnt = std::min(g, batch - c0);

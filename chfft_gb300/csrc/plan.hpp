@@ -22,6 +22,20 @@ struct Fail {
 void cuda_check(cudaError_t e, const char* what);
 #define CHFFT_CUDA(call) ::chfft::cuda_check((call), #call)
 
+// One page-locked int mapped into the device address space (cudaHostAlloc
+// mapped): kernels write it, the host reads it after a synchronisation.
+struct HostWord {
+  int* host = nullptr;
+  int* dev = nullptr;
+  HostWord() = default;
+  HostWord(const HostWord&) = delete;
+  HostWord& operator=(const HostWord&) = delete;
+  ~HostWord();
+  void ensure();
+  // The recorded code (0 if none), cleared.
+  int take();
+};
+
 // Owning device allocation.
 struct DevBuf {
   void* p = nullptr;
@@ -131,6 +145,14 @@ Geo col_geo(const Core& c, int ncols, int tpb_opt = 0, const PlanOpts& o = PlanO
 // Smallest 7-smooth M >= lo that the CTA engine runs cheapest (M * passes).
 long long bluestein_length(long long n, int dtype);
 
+// Polls a bounded device-side wait makes before it gives up: CHFFT_SPIN_LIMIT,
+// default 4,000,000 (about a second at ~0.25 us per poll).
+long long spin_limit();
+// Test hook: CHFFT_TEST_STALL=1 makes one dependency of each pipelined
+// four-step launch unreachable, so a bounded wait runs out and the call
+// reports CHFFT_ETIMEOUT (the kernels still return normally).
+int stall_test();
+
 // Whether plan-time specialised kernels are used for a launch of `elems`
 // elements (CHFFT_JIT policy, unless the plan's jit knob overrides it).
 bool want_specialised(long long elems, int jit_opt = -1);
@@ -146,11 +168,23 @@ struct BigCore {
   int n1 = 0, n2 = 0, tw_l = 0, tw_shift = 0;
   Core ca, cb;  // column core (n1), row core (n2)
   DevBuf lo, hi, chirp, bhat;
+  // Pipelined four-step (k_pipe.cuh): both passes in one persistent launch,
+  // for f32 non-Bluestein lengths whose split has a kernel shape. Stage
+  // twiddles of the (n/32, 32) pass orders of n1 and n2, and the pass-A
+  // tiles' twiddle tables.
+  bool pipe = false;
+  DevBuf pstw_a, pstw_b, ptw;
+  // Host-mapped error word the pipelined launch sets when a bounded wait
+  // gives up; read (and cleared) after the plan's stream is synchronised.
+  HostWord err;
   PlanOpts opts;
   bool build(long long n, int dtype, cudaStream_t s, const PlanOpts& o = PlanOpts{});  // false: unsupported
   FourStep fs() const;
   long long chunk(long long batch) const;                  // transforms per chunk
   long long work_elems(long long batch) const;             // complex workspace elements
+  // Pipelined launch parameters for `batch` transforms (ring slots, lead,
+  // L2 hints); false when the pipelined kernel does not apply.
+  bool pipe_params(long long batch, int* ring, int* lead, int* hints) const;
   // batch contiguous sequences in -> out (distance n), workspace `work`.
   // max_chunk > 0 caps the transforms per chunk (a fixed-size workspace);
   // library_only skips plan-time specialised kernels.
@@ -159,7 +193,8 @@ struct BigCore {
   // Workspace bytes one transform needs.
   size_t work_bytes_per_transform() const { return (size_t)m * cplx_bytes(dtype) * (blue ? 2 : 1); }
   size_t device_bytes() const {
-    return ca.device_bytes() + cb.device_bytes() + lo.bytes + hi.bytes + chirp.bytes + bhat.bytes;
+    return ca.device_bytes() + cb.device_bytes() + lo.bytes + hi.bytes + chirp.bytes + bhat.bytes + pstw_a.bytes +
+           pstw_b.bytes + ptw.bytes;
   }
 };
 

@@ -343,6 +343,15 @@ struct PlanImpl {
     }
   }
 
+  // Throws CHFFT_ETIMEOUT when a bounded device-side wait of this plan's
+  // kernels gave up since the last check (the host-mapped word the
+  // pipelined four-step launch sets). Call after a synchronisation.
+  void check_waits() {
+    if (int code = big.err.take())
+      throw Fail{CHFFT_ETIMEOUT, "a device-side wait of the pipelined four-step launch gave up (code " +
+                                     std::to_string(code) + "); that launch's output is incomplete"};
+  }
+
   void exec(const MethodSpec& ms, const void* d_in, void* d_out, long long batch, cudaStream_t s) {
     if (batch <= 0) return;
     if (dtype == CHFFT_F32)
@@ -383,6 +392,7 @@ struct PlanImpl {
       if (ms_src && ms_dst) {
         exec(ms, ms_src, ms_dst, batch, s);
         CHFFT_CUDA(cudaStreamSynchronize(s));
+        check_waits();
         return;
       }
     }
@@ -395,6 +405,7 @@ struct PlanImpl {
       exec(ms, stage_in.p, stage_out.p, batch, s);
       if (ob) CHFFT_CUDA(cudaMemcpyAsync(dst, stage_out.p, ob, cudaMemcpyDeviceToHost, s));
       CHFFT_CUDA(cudaStreamSynchronize(s));
+      check_waits();
       return;
     }
     if (!copy_in) CHFFT_CUDA(cudaStreamCreateWithFlags(&copy_in, cudaStreamNonBlocking));
@@ -421,6 +432,7 @@ struct PlanImpl {
     }
     CHFFT_CUDA(cudaStreamSynchronize(copy_out));
     CHFFT_CUDA(cudaStreamSynchronize(s));
+    check_waits();
   }
 };
 

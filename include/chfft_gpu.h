@@ -131,6 +131,14 @@ CHFFT_API int chfft_execute_batch(chfft_plan plan, int method, const void* src, 
 CHFFT_API int chfft_execute_device(chfft_plan plan, int method, const void* d_src, void* d_dst, size_t batch,
                                    void* stream);
 
+/* Waits for `stream`, then reports CHFFT_ETIMEOUT if a bounded device-side
+ * wait in one of this plan's launches gave up since the last check (the
+ * launch then returned without hanging and its output is incomplete; the
+ * pipelined four-step launch of CFft1D plans waits on other CTAs' tiles).
+ * The host-memory calls make this check themselves. No counterpart in the
+ * reference: chfft's transforms are synchronous CPU calls. */
+CHFFT_API int chfft_plan_wait(chfft_plan plan, void* stream);
+
 /* Device execution that allocates nothing. No counterpart in the reference
  * (chfft allocates a new Vec for every result).
  *

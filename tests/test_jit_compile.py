@@ -4,8 +4,8 @@ The library compiles these at plan time on the GPU host (csrc/jit.cu), and a
 failed compile there falls back to the run-time-stage library kernels, so a
 header change that breaks them would only show as slower plans. This test
 hands NVRTC the same headers, options and name expressions (the instances
-of the benchmark's plans, the four-step passes, the fused four-step launch
-and the Bluestein middle pass) and checks that each compiles, and that the
+of the benchmark's plans, the four-step passes and the Bluestein middle
+pass) and checks that each compiles, and that the
 hot ones stay free of register spills. NVRTC needs no GPU.
 """
 import ctypes
@@ -61,7 +61,6 @@ CASES = [
     (f"&chfft::kern::k_cols_tw<float, {A_2P20}, 8>", True),
     (f"&chfft::kern::k_rows_t<float, {A_2P20}, 0>", True),
     (f"&chfft::kern::k_rows_t<float, {A_2P20}, 2>", False),
-    (f"&chfft::kern::k_fourstep_fused<float, {A_2P20}, {A_2P20}, 12, 4>", True),
     ("&chfft::kern::k_rows_bb<float, chfft::StatCore<false,true,true,512,512,8,546,16,256,4,0,16,16,2>, 3>", True),
     ("&chfft::kern::k_rows_bb<double, chfft::StatCore<false,true,false,256,256,4,274,16,256,1,0,16,16>, 7>", False),
 ]

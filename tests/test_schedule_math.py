@@ -4,9 +4,9 @@ numpy / Python and checked on small cases (the GPU tests check the kernels).
 - three-pass four-step Bluestein of the uneven batch (k_batch.cu FS_A,
   FS_BB, FS_C): forward FFT with k = k1 + n1 k2, spectrum product, inverse
   FFT split as m = m2 + n2 m1 so its first pass runs over the same rows;
-- the fused four-step launch's ticket order (k_complex.cuh
-  k_fourstep_fused): every tile appears once, and every wait is on tickets
-  taken earlier, for any batch, lead and ring.
+- the pipelined four-step launch's ticket order (k_pipe.cuh decode): every
+  tile appears once, and every wait is on tickets taken earlier, for any
+  batch, lead and ring the host allows (plan.cu BigCore::pipe_params).
 """
 import numpy as np
 import pytest
@@ -58,7 +58,7 @@ def test_three_pass_bluestein_matches_dft(n, n1, n2):
 
 
 def decode(t, count, ta, tb, lead):
-    """Ticket t -> (is_a, transform, tile), as k_fourstep_fused decodes it."""
+    """Ticket t -> (is_a, transform, tile), as k_pipe.cuh decode() does."""
     per, pairs = ta + tb, count - lead
     if t < lead * ta:
         k = t // ta
@@ -75,9 +75,9 @@ def decode(t, count, ta, tb, lead):
 @pytest.mark.parametrize("count", [1, 2, 3, 5, 9])
 @pytest.mark.parametrize("ta,tb", [(1, 1), (3, 2), (4, 7)])
 @pytest.mark.parametrize("lead,ring", [(1, 2), (2, 3), (2, 4), (3, 5), (4, 4)])
-def test_fused_ticket_order(count, ta, tb, lead, ring):
-    # the host clamps as plan.cu does
-    lead = min(lead, count)
+def test_pipe_ticket_order(count, ta, tb, lead, ring):
+    # the host clamps as BigCore::pipe_params does
+    lead = max(1, min(lead, count))
     ring = min(max(ring, lead + 1), count)
     pos = {}
     for t in range(count * (ta + tb)):
