@@ -63,7 +63,7 @@ struct PipeArgs {
 
 constexpr int kConsumers = 256;  // eight consumer warps
 constexpr int kConsumerWarps = kConsumers / 32;
-constexpr int kThreads = 288;    // plus the producer warp
+constexpr int kThreads = 320;    // plus the producer warp and the reporter warp
 constexpr int kTileElems = 8192; // complex elements per tile (64 KiB)
 
 // Exchange-buffer stride: >= n + n/32 (one pad slot per 32 elements) and
@@ -99,7 +99,9 @@ struct Shape {
   // per stage: the pass-A tile's twiddle tables atab[32][WA], wtab[N1/32][WA]
   static constexpr int TABS = 32 * WA + (N1 / 32) * WA;
   static constexpr int OFF_BAR = OFF_TAB + 2 * TABS * 8;
-  static constexpr int SMEM = OFF_BAR + 64 + 1024;  // + alignment slack
+  // barriers full[2] and empty[2], the fill log[8] and done counts[8], the
+  // producer's and the reporter's fill counts
+  static constexpr int SMEM = OFF_BAR + 192 + 1024;  // + alignment slack
   static_assert(N1 >= 256 && N1 <= 1024 && N2 >= 256 && N2 <= 1024, "tile shapes cover 256..1024");
 };
 
@@ -216,70 +218,51 @@ __device__ __forceinline__ void decode(long long t, long long count, int lead, b
 }
 
 // ------------------------------------------------------------ producer
-// Completion reports of the tiles this CTA's consumers run. A consumer warp
-// that is done with a tile only arrives on the stage's `empty` barrier; the
-// producer thread sees the phase complete and reports the tile to the other
-// CTAs (proxy fence for the ring rows, release fence, one atomic add). The
-// consumers' stores happen before their arrival, the arrival before the
-// producer's wait, the wait before its release: the report covers them.
-struct Pending {
-  long long k[2];  // transform of the tile in each stage, -1 if reported
-  bool is_a[2];
-  unsigned par[2]; // parity of the stage's `empty` phase that ends the tile
+// Fill u of the launch (u = 0, 1, ...) goes to stage u % 2, its ticket to
+// log[u % kLog]; the consumers and the reporter walk the fills in the same
+// order. The producer refills a stage once its consumers are done with it
+// (the `empty` barrier); the reporter follows behind, up to kLog fills, and
+// publishes finished tiles to the other CTAs.
+constexpr int kLog = 8;
+struct Ctl {
+  unsigned long long* full;   // [2]: the producer's arrival + the copies' bytes
+  unsigned long long* empty;  // [2]: one arrival per consumer warp
+  long long* log;             // [kLog]: ticket of each fill, -1 ends the launch
+  int* done;                  // [kLog]: consumer warps done with the fill
+  volatile int* filled;       // fills made (the log entry is written first)
+  volatile int* reported;     // fills published by the reporter
 };
-
-__device__ __forceinline__ void report_tile(const PipeArgs& a, Pending& p, int q) {
-  if (p.is_a[q]) fence_proxy_async_global();  // the ring rows are read next by bulk copies
-  __threadfence();
-  atomicAdd(p.is_a[q] ? a.done_a + p.k[q] : a.done_b + p.k[q], 1);
-  p.k[q] = -1;
-}
-
-// Reports every tile whose consumers are done (never waits).
-__device__ __forceinline__ void report_finished(const PipeArgs& a, Pending& p, unsigned long long* empty) {
-#pragma unroll
-  for (int q = 0; q < 2; q++)
-    if (p.k[q] >= 0 && mbar_test(&empty[q], p.par[q])) report_tile(a, p, q);
-}
 
 // The producer: one thread takes tickets (one ahead, so the atomic's
 // latency overlaps the current tile), waits for dependencies (a counter seen
-// complete once is not polled again), issues the copies and reports
-// finished tiles. A pass-A tile's copy brings the tile's twiddle tables
-// along (plan-time, FP64 rounded once):
+// complete once is not polled again) and issues the copies. A pass-A tile's
+// copy brings the tile's twiddle tables along (plan-time, FP64 rounded
+// once):
 //   atab[r][t] = w_N^(c R0 r),  wtab[j][t] = w_N^(c j),  c = c0 + t,
 // so the consumers' inter-pass twiddle w_N^(c k1) (k1 = j + R0 r) is two
 // shared loads and one product.
 template <int N1, int N2>
 __device__ __forceinline__ void producer(const TensorMap* tin, const PipeArgs& a, float2* stage, float2* tabs,
-                                         unsigned long long* full, unsigned long long* empty, long long* task) {
+                                         const Ctl& c) {
   using S = Shape<N1, N2>;
   constexpr int W = S::WA;
   constexpr unsigned kTabBytes = S::TABS * 8;
   const long long total = a.count * (long long)(S::TA + S::TB);
   const unsigned long long pol_in = a.hints ? policy_first() : policy_normal();
   const unsigned long long pol_ring = a.hints ? policy_last() : policy_normal();
-  int s = 0;
-  unsigned use[2] = {0u, 0u};
-  Pending pend;
-  pend.k[0] = pend.k[1] = -1;
   const int* seen = nullptr;  // dependency counter last seen complete
   long long next = (long long)atomicAdd(a.ticket, 1ull);
-  for (;;) {
-    bool end = false;
-    // The stage must be free: its last tile finished (and is reported).
-    bool free_stage = true;
-    for (long long it = 0; use[s] > 0 && !mbar_test(&empty[s], (use[s] - 1) & 1u); it++) {
-      report_finished(a, pend, empty);
-      if (it >= a.spin_limit) {
-        report(a, 4);
-        end = true;
-        free_stage = false;
-        break;
-      }
+  for (long long u = 0;; u++) {
+    const int s = (int)(u & 1);
+    // The stage's previous fill (u - 2) is consumed, and the log slot's
+    // previous fill (u - kLog) is published.
+    bool free_stage = u < 2 || mbar_wait(&c.empty[s], (unsigned)(((u - 2) >> 1) & 1), 16 * a.spin_limit);
+    for (long long it = 0; free_stage && *c.reported < u - kLog + 1; it++) {
+      if (it >= 16 * a.spin_limit) free_stage = false;
       __nanosleep(64);
     }
-    report_finished(a, pend, empty);
+    bool end = !free_stage;
+    if (!free_stage) report(a, 4);
     const long long t = next;
     if (!end) end = t >= total || *(volatile int*)a.err != 0;
     bool is_a = true;
@@ -291,7 +274,6 @@ __device__ __forceinline__ void producer(const TensorMap* tin, const PipeArgs& a
       const int need = (is_a ? S::TB : S::TA) + (!is_a && k == 0 && a.stall > 0 ? 1 : 0);
       if (w && w != seen) {
         for (long long it = 0; ld_acquire(w) < need; it++) {
-          report_finished(a, pend, empty);  // a dependency may be a tile of this CTA
           if (it >= a.spin_limit || *(volatile int*)a.err) {
             report(a, 3);
             end = true;
@@ -304,47 +286,98 @@ __device__ __forceinline__ void producer(const TensorMap* tin, const PipeArgs& a
     }
     if (end) {
       // The end marker goes to the next stage when it is free; the
-      // consumers leave when they reach it.
+      // consumers and the reporter leave when they reach it. Copies already
+      // issued are consumed before that.
       if (free_stage) {
-        task[s] = -1;
-        mbar_arrive(&full[s]);
-      }
-      // Tiles still running are reported when they finish, and no copy is
-      // left in flight (bounded waits).
-      for (int q = 0; q < 2; q++) {
-        if (pend.k[q] >= 0) {
-          if (mbar_wait(&empty[q], pend.par[q], 8 * a.spin_limit)) report_tile(a, pend, q);
-        } else if ((q != s || !free_stage) && use[q] > 0) {
-          mbar_wait(&full[q], (use[q] - 1) & 1u, a.spin_limit);
-        }
+        c.log[u % kLog] = -1;
+        __threadfence_block();
+        *c.filled = (int)(u + 1);
+        mbar_arrive(&c.full[s]);
       }
       return;
     }
     float2* dst = stage + s * kTileElems;
-    task[s] = t;
-    pend.k[s] = k;
-    pend.is_a[s] = is_a;
-    pend.par[s] = use[s] & 1u;
+    c.log[u % kLog] = t;
+    __threadfence_block();
+    *c.filled = (int)(u + 1);
     if (is_a) {
-      mbar_expect_tx(&full[s], kTileElems * 8 + kTabBytes);
+      mbar_expect_tx(&c.full[s], kTileElems * 8 + kTabBytes);
 #pragma unroll
       for (int q = 0; q < N1 / S::BOXR; q++)
-        tma_load_2d(dst + q * S::BOXR * W, tin, (int)tile * W, (int)(k * N1 + q * S::BOXR), &full[s], pol_in);
-      bulk_load(tabs + s * S::TABS, a.tiles_tw + tile * S::TABS, kTabBytes, &full[s], pol_ring);
+        tma_load_2d(dst + q * S::BOXR * W, tin, (int)tile * W, (int)(k * N1 + q * S::BOXR), &c.full[s], pol_in);
+      bulk_load(tabs + s * S::TABS, a.tiles_tw + tile * S::TABS, kTabBytes, &c.full[s], pol_ring);
     } else {
       // The ring rows were written through the generic proxy by other CTAs
       // (release / acquire on done_a); the bulk copy reads them through the
       // async proxy.
       fence_proxy_async_global();
-      mbar_expect_tx(&full[s], kTileElems * 8);
+      mbar_expect_tx(&c.full[s], kTileElems * 8);
       const float2* src = a.ring + (k % a.ring_slots) * (long long)S::N + tile * (long long)S::WB * N2;
-      bulk_load(dst, src, kTileElems * 8, &full[s], pol_ring);
+      bulk_load(dst, src, kTileElems * 8, &c.full[s], pol_ring);
     }
-    // The phase's one arrival: releases task[s]; the phase completes when
-    // the copies' bytes have landed as well.
-    mbar_arrive(&full[s]);
-    use[s]++;
-    s ^= 1;
+    // The phase's one arrival: releases the log entry to the consumers; the
+    // phase completes when the copies' bytes have landed as well.
+    mbar_arrive(&c.full[s]);
+  }
+}
+
+// ------------------------------------------------------------ reporter
+// Publishes finished tiles to the other CTAs. Each consumer warp that is
+// done with fill u adds one to done[u % kLog] (release, CTA scope); when it
+// reaches kConsumerWarps the reporter (acquire) has seen all of the tile's
+// stores, and one acq_rel fence at GPU scope releases them before the
+// tile's counter goes up (plus a proxy fence for ring rows, which bulk
+// copies read next). The fence waits for those stores to reach L2
+// (microseconds), so it runs here, off the producer's path, once for every
+// tile that finished meanwhile.
+template <int TA, int TB>
+__device__ __forceinline__ void reporter(const PipeArgs& a, const Ctl& c) {
+  const long long limit = 32 * a.spin_limit;
+  long long u = 0;
+  for (;;) {
+    long long it = 0;
+    while (*c.filled <= u) {
+      if (++it > limit) return;
+      __nanosleep(64);
+    }
+    __threadfence_block();
+    if (c.log[u % kLog] < 0) return;
+    // Every fill from u on whose consumers are done.
+    long long v = u;
+    bool any_a = false;
+    for (it = 0;;) {
+      if (v < *c.filled) {
+        __threadfence_block();
+        const long long t = c.log[v % kLog];
+        int d;
+        asm volatile("ld.acquire.cta.shared::cta.b32 %0, [%1];" : "=r"(d) : "r"(su32(c.done + v % kLog)) : "memory");
+        if (t >= 0 && d == kConsumerWarps) {
+          bool is_a;
+          long long k, tile;
+          decode<TA, TB>(t, a.count, a.lead, is_a, k, tile);
+          any_a |= is_a;
+          v++;
+          continue;
+        }
+      }
+      if (v > u) break;
+      if (++it > limit) {
+        report(a, 6);
+        return;
+      }
+      __nanosleep(64);
+    }
+    if (any_a) fence_proxy_async_global();  // the ring rows are read next by bulk copies
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");
+    for (; u < v; u++) {
+      bool is_a;
+      long long k, tile;
+      decode<TA, TB>(c.log[u % kLog], a.count, a.lead, is_a, k, tile);
+      atomicAdd(is_a ? a.done_a + k : a.done_b + k, 1);
+      c.done[u % kLog] = 0;
+    }
+    __threadfence_block();
+    *c.reported = (int)u;
   }
 }
 
@@ -434,11 +467,14 @@ __device__ __forceinline__ void tile_b(const PipeArgs& a, const float2* stg, flo
 }
 
 // A consumer warp is done with a tile: it frees the stage (its data was
-// read in the first pass, its twiddle tables in the second); the producer
-// reports the tile once all eight warps have arrived.
-__device__ __forceinline__ void finish_tile(unsigned long long* empty) {
-  __syncwarp();  // orders every lane's accesses before lane 0's release
-  if ((threadIdx.x & 31) == 0) mbar_arrive(empty);
+// read in the first pass, its twiddle tables in the second) and counts
+// itself done for the reporter (release: its stores come first).
+__device__ __forceinline__ void finish_tile(unsigned long long* empty, int* done) {
+  __syncwarp();  // orders every lane's accesses before lane 0's releases
+  if ((threadIdx.x & 31) == 0) {
+    mbar_arrive(empty);
+    asm volatile("red.release.cta.shared::cta.add.s32 [%0], 1;" ::"r"(su32(done)) : "memory");
+  }
 }
 
 template <int N1, int N2, bool BACK>
@@ -451,9 +487,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_pipe(const __grid_constant__ Te
   float2* stwa = reinterpret_cast<float2*>(base + S::OFF_STWA);
   float2* stwb = reinterpret_cast<float2*>(base + S::OFF_STWB);
   float2* tabs = reinterpret_cast<float2*>(base + S::OFF_TAB);
-  unsigned long long* full = reinterpret_cast<unsigned long long*>(base + S::OFF_BAR);
-  unsigned long long* empty = full + 2;
-  long long* task = reinterpret_cast<long long*>(full + 4);
+  Ctl c;
+  c.full = reinterpret_cast<unsigned long long*>(base + S::OFF_BAR);
+  c.empty = c.full + 2;
+  c.log = reinterpret_cast<long long*>(c.full + 4);
+  c.done = reinterpret_cast<int*>(c.log + kLog);
+  c.filled = c.done + kLog;
+  c.reported = c.filled + 1;
   const int tid = threadIdx.x;
   // Radix-32 stage twiddles (the second pass's block of the stage tables).
   for (int i = tid; i < S::NSTWA; i += kThreads) stwa[i] = a.stw_a[N1 / 32 - 1 + i];
@@ -462,25 +502,28 @@ __global__ void __launch_bounds__(kThreads, 1) k_pipe(const __grid_constant__ Te
   if (tid == 0) {
     // full: the producer's one arrival per fill plus the copies' bytes;
     // empty: one arrival per consumer warp when it is done with the tile.
-    mbar_init(&full[0], 1);
-    mbar_init(&full[1], 1);
-    mbar_init(&empty[0], kConsumerWarps);
-    mbar_init(&empty[1], kConsumerWarps);
+    mbar_init(&c.full[0], 1);
+    mbar_init(&c.full[1], 1);
+    mbar_init(&c.empty[0], kConsumerWarps);
+    mbar_init(&c.empty[1], kConsumerWarps);
+    for (int q = 0; q < kLog; q++) c.done[q] = 0;
+    *c.filled = 0;
+    *c.reported = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
   if (tid >= kConsumers) {
-    if (tid == kConsumers) producer<N1, N2>(&tin, a, stage, tabs, full, empty, task);
+    if (tid == kConsumers) producer<N1, N2>(&tin, a, stage, tabs, c);
+    if (tid == kConsumers + 32) reporter<S::TA, S::TB>(a, c);
     return;
   }
   const unsigned long long pol_ring = a.hints ? policy_last() : policy_normal();
   const unsigned long long pol_out = a.hints ? policy_first() : policy_normal();
-  int s = 0;
-  unsigned ph[2] = {0u, 0u};
-  for (;;) {
+  for (long long u = 0;; u++) {
+    const int s = (int)(u & 1);
     // Longer than the producer's waits, so a producer that gives up reaches
     // the consumers with its end marker first.
-    const bool ok = mbar_wait(&full[s], ph[s], 8 * a.spin_limit);
+    const bool ok = mbar_wait(&c.full[s], (unsigned)((u >> 1) & 1), 16 * a.spin_limit);
     // One barrier per tile boundary: every consumer has finished the
     // previous tile (the exchange buffer is free), and all agree whether to
     // leave.
@@ -489,7 +532,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pipe(const __grid_constant__ Te
       if (tid == 0) report(a, 5);
       return;
     }
-    const long long t = task[s];
+    const long long t = c.log[u % kLog];
     if (t < 0) return;
     bool is_a;
     long long k, tile;
@@ -499,9 +542,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pipe(const __grid_constant__ Te
       tile_a<N1, N2, BACK>(a, stg, xch, stwa, tabs + s * S::TABS, k, (int)tile * S::WA, tid, pol_ring);
     else
       tile_b<N1, N2, BACK>(a, stg, xch, N1 == N2 ? stwa : stwb, k, (int)tile * S::WB, tid, pol_out);
-    finish_tile(&empty[s]);
-    ph[s] ^= 1u;
-    s ^= 1;
+    finish_tile(&c.empty[s], c.done + u % kLog);
   }
 }
 
