@@ -382,14 +382,23 @@ __device__ __forceinline__ void reporter(const PipeArgs& a, const Ctl& c) {
 }
 
 // ------------------------------------------------------------ consumer tiles
+// A consumer warp has read everything it needs from the stage (the data in
+// the first pass, the tile's twiddles into registers): it frees the stage,
+// so the producer's copy of the tile after next overlaps the second pass.
+__device__ __forceinline__ void release_stage(unsigned long long* empty) {
+  __syncwarp();  // every lane's reads come before lane 0's arrival
+  if ((threadIdx.x & 31) == 0) mbar_arrive(empty);
+}
+
 // Pass A tile: columns c0 .. c0 + WA - 1 of transform k. The stage holds the
 // tile as [n1][t] (TMA box rows); the first pass is N1/32-point butterflies
 // (K0 per thread) over n1 with stride 32, the second radix 32 with stage
 // twiddles w_N1^(j r); the result row k1 = j + (N1/32) r goes to the ring
-// times scale w_N^(k1 c) (the tile's tables, copied with its data).
+// times scale w_N^(k1 c) (the tile's tables, copied with its data). The
+// stage is released after the first pass.
 template <int N1, int N2, bool BACK>
 __device__ __forceinline__ void tile_a(const PipeArgs& a, const float2* stg, float2* xch, const float2* stw,
-                                       const float2* atab, long long k, int c0, int tid,
+                                       const float2* atab, long long k, int c0, int tid, unsigned long long* empty,
                                        unsigned long long pol_ring) {
   using S = Shape<N1, N2>;
   constexpr int W = S::WA, R0 = N1 / 32, K0 = 32 / R0, LD = S::LDA;
@@ -413,19 +422,26 @@ __device__ __forceinline__ void tile_a(const PipeArgs& a, const float2* stg, flo
       for (int r = 0; r < R0; r++) xch[t * LD + xch_pad(j * R0 + r)] = v[kk][r];
     }
   }
-  consumers_sync();
+  // This thread's inter-pass twiddles scale w_N^(c (j + R0 r)), read now so
+  // the stage (data and tables) is free before the second pass.
   const int t = tid % W, j = tid / W;
+  float2 tw[32];
+  {
+    const float2 wj = cscale(wtab[j * W + t], a.scale);
+#pragma unroll
+    for (int r = 0; r < 32; r++) tw[r] = cmul(wj, atab[r * W + t]);
+  }
+  release_stage(empty);
+  consumers_sync();
   float2 u[32];
 #pragma unroll
   for (int r = 0; r < 32; r++) u[r] = xch[t * LD + xch_pad(j + R0 * r)];
 #pragma unroll
   for (int r = 1; r < 32; r++) u[r] = cmul(u[r], stw[(r - 1) * R0 + j]);
   Dft<32>::run(u);
-  const float2 wj = cscale(wtab[j * W + t], a.scale);
   float2* dst = a.ring + (k % a.ring_slots) * (long long)S::N + c0 + t;
 #pragma unroll
-  for (int r = 0; r < 32; r++)
-    st_hint(dst + (long long)(j + R0 * r) * N2, cmul(u[r], cmul(wj, atab[r * W + t])), pol_ring);
+  for (int r = 0; r < 32; r++) st_hint(dst + (long long)(j + R0 * r) * N2, cmul(u[r], tw[r]), pol_ring);
 }
 
 // Pass B tile: rows r0 .. r0 + WB - 1 of transform k's intermediate, held
@@ -434,7 +450,8 @@ __device__ __forceinline__ void tile_a(const PipeArgs& a, const float2* stg, flo
 // X[r0 + t + N1 k2] is contiguous over t.
 template <int N1, int N2, bool BACK>
 __device__ __forceinline__ void tile_b(const PipeArgs& a, const float2* stg, float2* xch, const float2* stw,
-                                       long long k, int r0, int tid, unsigned long long pol_out) {
+                                       long long k, int r0, int tid, unsigned long long* empty,
+                                       unsigned long long pol_out) {
   using S = Shape<N1, N2>;
   constexpr int W = S::WB, R0 = N2 / 32, K0 = 32 / R0, LD = S::LDB;
   {
@@ -453,6 +470,7 @@ __device__ __forceinline__ void tile_b(const PipeArgs& a, const float2* stg, flo
       for (int r = 0; r < R0; r++) xch[t * LD + xch_pad(j * R0 + r)] = v[kk][r];
     }
   }
+  release_stage(empty);
   consumers_sync();
   const int t = tid % W, j = tid / W;
   float2 u[32];
@@ -466,15 +484,12 @@ __device__ __forceinline__ void tile_b(const PipeArgs& a, const float2* stg, flo
   for (int r = 0; r < 32; r++) st_hint(dst + (long long)(j + R0 * r) * N1, BACK ? cconj(u[r]) : u[r], pol_out);
 }
 
-// A consumer warp is done with a tile: it frees the stage (its data was
-// read in the first pass, its twiddle tables in the second) and counts
-// itself done for the reporter (release: its stores come first).
-__device__ __forceinline__ void finish_tile(unsigned long long* empty, int* done) {
-  __syncwarp();  // orders every lane's accesses before lane 0's releases
-  if ((threadIdx.x & 31) == 0) {
-    mbar_arrive(empty);
+// A consumer warp is done with a tile: it counts itself done for the
+// reporter (release: its stores come first).
+__device__ __forceinline__ void finish_tile(int* done) {
+  __syncwarp();  // orders every lane's stores before lane 0's release
+  if ((threadIdx.x & 31) == 0)
     asm volatile("red.release.cta.shared::cta.add.s32 [%0], 1;" ::"r"(su32(done)) : "memory");
-  }
 }
 
 template <int N1, int N2, bool BACK>
@@ -539,10 +554,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_pipe(const __grid_constant__ Te
     decode<S::TA, S::TB>(t, a.count, a.lead, is_a, k, tile);
     const float2* stg = stage + s * kTileElems;
     if (is_a)
-      tile_a<N1, N2, BACK>(a, stg, xch, stwa, tabs + s * S::TABS, k, (int)tile * S::WA, tid, pol_ring);
+      tile_a<N1, N2, BACK>(a, stg, xch, stwa, tabs + s * S::TABS, k, (int)tile * S::WA, tid, &c.empty[s], pol_ring);
     else
-      tile_b<N1, N2, BACK>(a, stg, xch, N1 == N2 ? stwa : stwb, k, (int)tile * S::WB, tid, pol_out);
-    finish_tile(&c.empty[s], c.done + u % kLog);
+      tile_b<N1, N2, BACK>(a, stg, xch, N1 == N2 ? stwa : stwb, k, (int)tile * S::WB, tid, &c.empty[s], pol_out);
+    finish_tile(c.done + u % kLog);
   }
 }
 
