@@ -1,23 +1,29 @@
 #!/usr/bin/env python3
-"""Benchmark: batched FFT GFLOP/s (5 N log2 N) on the mixed-radix + Bluestein
-f32 workload, and HBM GB/s with its roofline fraction.
+"""Benchmark: batched FFT GFLOP/s (5 N log2 N) and HBM GB/s with the roofline
+fraction, plus the tensor-core form against the FP32 path at its rel-L2.
 
-Workload ("step" = one forward pass over the batch, all f32):
-  - CFft1D 4096 x N=1000  (2^3 5^3, mixed radix), complex N(0,1)
-  - CFft1D 4096 x N=1009  (prime, Bluestein / Chirp-Z), complex N(0,1)
-  - CFft2D 2048 x 2048,   complex uniform[-1, 1)
-Inputs are seeded synthetic data (the reference has no dataset); they sit in
-HBM before the timed region. Each timed step is bracketed by CUDA events on
-the launch stream and the L2 is flushed (256 MiB memset) between steps,
-outside the events. `e2e` runs the same workload through the C ABI's
-host-pointer entry point (chfft_execute_batch) from pinned host memory, so
-every step includes the H2D copy of the inputs and the D2H copy of the
-outputs.
+Default workload (the metric's precision configuration; "step" = one
+forward pass over both parts, f32 in and out):
+  - CFft1D 64 x N=2^20     (four-step: one pipelined launch)
+  - CFft1D 16384 x N=4096  (one CTA per transform)
+complex N(0,1) with 1% of the entries (seeded Bernoulli) scaled x1e3; both
+inputs are 512 MiB, larger than L2, and sit in HBM before the timed region.
+Each step is bracketed by CUDA events on the launch stream. `value` is the
+plain FP32 path; `tc_vs_fp32` times the tensor-core form (radix-16 passes as
+FP16 / BF16 split-operand products with FP32 accumulation) on the same plans
+and inputs, each with its relative L2 error against numpy's FP64 FFT.
+`e2e` runs the same workload through the C ABI's host-pointer entry point
+(chfft_execute_batch) from pinned host memory, copies included.
+`roofline` is the longest single launch (the 2^20 x 64 pipelined launch):
+its algorithmic bytes (one read + one write) over its event time against
+the measured HBM copy bandwidth; `traffic` is its DRAM read + write bytes
+from the committed ncu summary.
 
-`--impl reference` times the CPU oracle (a C++ restatement of chfft's
-algorithm; the Rust crate cannot be built here) on the same workload with
-every host thread: one plan per thread over each 1-D batch, the 2-D
-transform on one thread as chfft's CFft2D runs.
+`--workload batch` is the other f32 configuration (4096 x N=1000, 4096 x
+N=1009 Chirp-Z, CFft2D 2048 x 2048); `uneven`, `costmodel` and `f64` the
+rest. `--impl reference` times the CPU oracle (a C++ restatement of chfft's
+algorithm; the Rust crate cannot be built here) on a bounded sample of the
+same workload with every host thread.
 
 Multi-GPU: every rank runs the workload on its own GPU (independent
 replicas, no collective); value = all ranks' work / max-over-ranks time.
@@ -565,134 +571,236 @@ def run_uneven(args):
     return 0
 
 
-def run_large(args):
+# ---------------------------------------------------------------------------- default: precision configuration
+PREC_WORKLOAD = ("cfft1d f32 64 x N=2^20 (pipelined four-step) + cfft1d f32 16384 x N=4096, forward; "
+                 "complex N(0,1), 1% of entries x1e3")
+PREC_PARTS = [("c2c_2^20x64", 1 << 20, 64), ("c2c_4096x16384", 4096, 16384)]
+PREC_SMALL = [("c2c_2^20x16", 1 << 20, 16), ("c2c_4096x4096", 4096, 4096)]
+
+
+def prec_input(n, batch, seed):
+    """Complex N(0,1), 1% of the entries (seeded Bernoulli) scaled x1e3."""
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal((batch, n), dtype=np.float32) + 1j * rng.standard_normal((batch, n), dtype=np.float32)
+    x[rng.random((batch, n)) < 0.01] *= 1e3
+    return x.astype(np.complex64)
+
+
+def prec_flops(parts):
+    return sum(5.0 * n * math.log2(n) * b for _, n, b in parts)
+
+
+def prec_bytes(parts):
+    return sum(16.0 * n * b for _, n, b in parts)
+
+
+def rel_rows(x, y, rows):
+    """Worst relative L2 error of rows of y against numpy's FP64 FFT of x."""
+    worst = 0.0
+    for r in rows:
+        ref = np.fft.fft(x[r].astype(np.complex128))
+        worst = max(worst, float(np.linalg.norm(y[r].astype(np.complex128) - ref) / np.linalg.norm(ref)))
+    return worst
+
+
+def prec_cpu(parts, reps, threads):
+    """The oracle on a bounded sample of each part (2 transforms of 2^20, 256
+    of 4096), all host threads; GFLOP/s of the sample."""
+    import oracle
+
+    sample = [(n, min(b, 2 if n > 65536 else 256)) for _, n, b in parts]
+    xs = [prec_input(n, b, 40 + k) for k, (n, b) in enumerate(sample)]
+    flops = sum(5.0 * n * math.log2(n) * b for n, b in sample)
+    per = []
+    for it in range(reps + 1):
+        t = 0.0
+        for x in xs:
+            _, secs = oracle.cfft1d(x, "forward", nthreads=threads, timing=True)
+            t += secs
+        if it:
+            per.append(t)
+    t = statistics.median(per)
+    desc = " + ".join(f"{b} x N={n}" for n, b in sample)
+    return flops / t / 1e9, t, desc
+
+
+def run_precision_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    parts = PREC_SMALL if args.small else PREC_PARTS
+    v, t, desc = prec_cpu(parts, max(1, min(args.steps, 5)), threads)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": "GFLOP/s", "n_gpus": world,
+        "steps": max(1, min(args.steps, 5)), "warmup": 1, "ms_per_step": round(t * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic N(0,1) complex with 1% of entries x1e3 (seeded)",
+        "config": {"workload": PREC_WORKLOAD, "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": round(v, 3), "unit": "GFLOP/s", "cores": threads, "kind": "port",
+                         "sample": f"{desc} per step (bounded sample of the workload), one oracle call per part "
+                                   "over all host threads"},
+        "e2e": {"value": round(v, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_precision(args, rank, world, local_rank):
     import torch
 
     import chfft_gb300 as cg
-
-    dev = torch.device("cuda", 0)
-    stream = torch.cuda.current_stream(dev)
-    sptr = stream.cuda_stream
-    parts = [("c2c_2^20x64", 1 << 20, 64), ("c2c_4096x16384", 4096, 16384)]
-    if args.small:  # the profiling case: the same kernels on 128 / 256 MiB inputs
-        parts = [("c2c_2^20x16", 1 << 20, 16), ("c2c_4096x8192", 4096, 8192)]
-    rng = np.random.default_rng(4)
-    plans, d_in, d_out, h_in, h_out = [], [], [], [], []
-    worst = 0.0
-    for name, n, batch in parts:
-        x = rng.standard_normal((batch, n), dtype=np.float32) + 1j * rng.standard_normal((batch, n), dtype=np.float32)
-        spikes = rng.random((batch, n)) < 0.01
-        x[spikes] *= 1e3
-        x = x.astype(np.complex64)
-        p = cg.CFft1D.with_len(n, np.float32)
-        plans.append(p)
-        t = torch.from_numpy(x.view(np.float32)).to(dev)
-        d_in.append(t)
-        d_out.append(torch.empty_like(t))
-        h_in.append(torch.from_numpy(x.view(np.float32)).pin_memory())
-        h_out.append(torch.empty_like(h_in[-1]).pin_memory())
-        p.execute_device("forward", t.data_ptr(), d_out[-1].data_ptr(), batch, sptr)
-        torch.cuda.synchronize()
-        y = d_out[-1].cpu().numpy().view(np.complex64)
-        for i in (0, batch - 1):
-            ref = np.fft.fft(x[i].astype(np.complex128))
-            worst = max(worst, float(np.linalg.norm(y[i] - ref) / np.linalg.norm(ref)))
-        del x
-    if worst > 1e-6:
-        raise SystemExit(f"large workload: rel-L2 {worst:.2e} > 1e-6")
-    clocks = ClockSampler(0).start()
-    part_ms = []
-    for i, (name, n, batch) in enumerate(parts):
-        part_ms.append(time_events(lambda: plans[i].execute_device("forward", d_in[i].data_ptr(), d_out[i].data_ptr(),
-                                                                    batch, sptr), args.steps, args.warmup, None, stream))
-    # The tensor-core form: radix-16 passes as FP16 / BF16 split-operand
-    # matrix products with FP32 accumulation, same plans, same inputs.
     from chfft_gb300 import tuning
 
-    tc_parts = {}
-    for i, (name, n, batch) in enumerate(parts):
-        row = {"fp32": {"ms": round(part_ms[i], 4), "rel_l2": None}}
-        for prec, label in ((0, "fp32"), (1, "tc_fp16x2"), (2, "tc_bf16x2"), (3, "tc_bf16x3")):
-            cfg = tuning.default_config()
-            cfg.tc_precision = prec
-            tuning.set_config(plans[i], cfg)
-            fn = lambda: plans[i].execute_device("forward", d_in[i].data_ptr(), d_out[i].data_ptr(), batch, sptr)  # noqa: E731
-            try:
-                fn()
-            except Exception as e:  # noqa: BLE001
-                row[label] = {"unavailable": str(e)}
-                continue
-            torch.cuda.synchronize()
-            err = 0.0
-            xs = h_in[i].numpy().view(np.complex64)
-            ys = d_out[i].cpu().numpy().view(np.complex64)
-            for r in (0, batch - 1):
-                ref = np.fft.fft(xs[r].astype(np.complex128))
-                err = max(err, float(np.linalg.norm(ys[r] - ref) / np.linalg.norm(ref)))
-            ms = part_ms[i] if prec == 0 else time_events(fn, args.steps, args.warmup, None, stream)
-            row[label] = {"ms": round(ms, 4), "rel_l2_vs_fp64": err,
-                          "speedup_vs_fp32": round(part_ms[i] / ms, 3)}
-        tuning.set_config(plans[i], tuning.default_config())
-        tc_parts[name] = row
-    # Four-step parts: the pipelined launch (default) against the two-launch
-    # path (CHFFT_PIPE=0), and the pipelined launch's schedules (--pipe).
-    forms = {}
-    for i, (name, n, batch) in enumerate(parts):
-        if plans[i].info().algorithm != 2:
-            continue
-        fn = lambda: plans[i].execute_device("forward", d_in[i].data_ptr(), d_out[i].data_ptr(), batch, sptr)  # noqa: E731
-        fn()
-        torch.cuda.synchronize()
-        ref_out = d_out[i].clone()
-        row = {"default_ms": round(part_ms[i], 4)}
-        for spec in ["0"] + [v for v in args.pipe.split(";") if v]:
-            os.environ["CHFFT_PIPE"] = spec
-            try:
-                d_out[i].zero_()
-                fn()
-                torch.cuda.synchronize()
-                diff = float((d_out[i] - ref_out).abs().max())
-                ms = time_events(fn, args.steps, args.warmup, None, stream)
-                row["two_launch" if spec == "0" else spec] = {"ms": round(ms, 4), "max_abs_diff_vs_default": diff,
-                                                                "default_speedup": round(ms / part_ms[i], 3)}
-            finally:
-                os.environ.pop("CHFFT_PIPE", None)
-        forms[name] = row
-        del ref_out
-    e2e_t = []
-    for i, (name, n, batch) in enumerate(parts):
-        for k in range(args.warmup + args.steps):
-            t0 = time.perf_counter()
-            rc = cg.lib().chfft_execute_batch(plans[i].handle, cg.METHODS["forward"], h_in[i].data_ptr(),
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+    parts = PREC_SMALL if args.small else PREC_PARTS
+    plans, d_in, d_out, h_in, h_out, fp32_err = [], [], [], [], [], []
+    for k, (name, n, batch) in enumerate(parts):
+        x = prec_input(n, batch, 4 + k)
+        p = cg.CFft1D.with_len(n, np.float32)
+        plans.append(p)
+        hi = torch.from_numpy(x.view(np.float32)).pin_memory()
+        h_in.append(hi)
+        h_out.append(torch.empty_like(hi).pin_memory())
+        d_in.append(hi.to(dev))
+        d_out.append(torch.empty_like(d_in[-1]))
+        p.execute_device("forward", d_in[-1].data_ptr(), d_out[-1].data_ptr(), batch, sptr)
+        p.wait(sptr)
+        y = d_out[-1].cpu().numpy().view(np.complex64)
+        fp32_err.append(rel_rows(x, y, (0, batch // 2, batch - 1)))
+        del x, y
+    if max(fp32_err) > 1e-6:
+        raise SystemExit(f"precision workload: FP32 rel-L2 {max(fp32_err):.2e} > 1e-6; refusing to time a wrong result")
+
+    def step(evs=None):
+        for i, (p, (_, _, batch)) in enumerate(zip(plans, parts)):
+            if evs is not None:
+                evs[i].record(stream)
+            p.execute_device("forward", d_in[i].data_ptr(), d_out[i].data_ptr(), batch, sptr)
+        if evs is not None:
+            evs[len(plans)].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local_rank).start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(len(plans) + 1)] for _ in range(args.steps)]
+    for k in range(args.steps):
+        step(ev[k])
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    for p in plans:
+        p.wait(sptr)  # a timed-out device wait would have left the output incomplete
+    part_ms = [[ev[k][i].elapsed_time(ev[k][i + 1]) for k in range(args.steps)] for i in range(len(plans))]
+    step_ms = [sum(part_ms[i][k] for i in range(len(plans))) for k in range(args.steps)]
+    ms = statistics.mean(step_ms)
+    means = [statistics.mean(pm) for pm in part_ms]
+
+    # end to end through the C ABI from pinned host memory
+    def e2e_step():
+        for i, (p, (_, _, batch)) in enumerate(zip(plans, parts)):
+            rc = cg.lib().chfft_execute_batch(p.handle, cg.METHODS["forward"], h_in[i].data_ptr(),
                                               h_out[i].data_ptr(), batch)
-            if rc:
-                raise SystemExit(cg.lib().chfft_last_error().decode())
-            if k >= args.warmup:
-                e2e_t.append((i, time.perf_counter() - t0))
+            if rc != 0:
+                raise SystemExit(f"chfft_execute_batch failed: {cg.lib().chfft_last_error().decode()}")
+
+    e2e_steps = max(2, min(args.steps, 10))
+    for _ in range(2):
+        e2e_step()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
     clk = clocks.stop()
-    e2e_s = sum(statistics.mean(t for j, t in e2e_t if j == i) for i in range(len(parts)))
-    flops = sum(5.0 * n * math.log2(n) * b for _, n, b in parts)
-    nbytes = sum(16.0 * n * b for _, n, b in parts)
-    ms = sum(part_ms)
+    ms, e2e_s = reduce_max([ms, e2e_s], world, device=dev)
+
+    # The tensor-core form on the same plans and inputs (rank 0 only; not timed
+    # inside the step).
+    tc = {}
+    forms = {}
+    if rank == 0:
+        for i, (name, n, batch) in enumerate(parts):
+            row = {"fp32": {"ms": round(means[i], 4), "rel_l2_vs_fp64": fp32_err[i]}}
+            xs = h_in[i].numpy().view(np.complex64)
+            for prec, label in ((1, "tc_fp16x2"), (2, "tc_bf16x2"), (3, "tc_bf16x3")):
+                cfg = tuning.default_config()
+                cfg.tc_precision = prec
+                tuning.set_config(plans[i], cfg)
+                fn = lambda: plans[i].execute_device("forward", d_in[i].data_ptr(), d_out[i].data_ptr(), batch, sptr)  # noqa: E731
+                try:
+                    fn()
+                    plans[i].wait(sptr)
+                except Exception as e:  # noqa: BLE001
+                    row[label] = {"unavailable": str(e)}
+                    continue
+                err = rel_rows(xs, d_out[i].cpu().numpy().view(np.complex64), (0, batch - 1))
+                t = time_events(fn, max(3, args.steps // 2), 2, None, stream)
+                row[label] = {"ms": round(t, 4), "rel_l2_vs_fp64": err, "speedup_vs_fp32": round(means[i] / t, 3)}
+            tuning.set_config(plans[i], tuning.default_config())
+            tc[name] = row
+            # four-step forms: the pipelined launch (default) against two launches
+            if plans[i].info().algorithm == 2:
+                fn = lambda: plans[i].execute_device("forward", d_in[i].data_ptr(), d_out[i].data_ptr(), batch, sptr)  # noqa: E731
+                os.environ["CHFFT_PIPE"] = "0"
+                try:
+                    forms[name] = {"pipelined_ms": round(means[i], 4),
+                                   "two_launch_ms": round(time_events(fn, max(3, args.steps // 2), 2, None, stream), 4)}
+                finally:
+                    os.environ.pop("CHFFT_PIPE", None)
+    if rank != 0:
+        return 0
+    # roofline: the longest single launch (part 0 is one pipelined launch)
+    dom = int(np.argmax(means))
+    dname, dn, db = parts[dom]
+    dom_bytes = 16.0 * dn * db
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured"
+    if not peak:
+        peak, peak_src = 6800.0, "fallback"
+    achieved = dom_bytes / (means[dom] * 1e-3) / 1e9
+    traffic = profiled_traffic().get(dname)
+    flops = prec_flops(parts)
+    nbytes = prec_bytes(parts)
+    kernel = {0: "k_pipe<1024,1024> (both four-step passes, one launch)", 1: "k_c2c N=4096"}.get(dom, dname)
     line = {
-        "metric": METRIC, "value": round(flops / (ms * 1e-3) / 1e9, 2), "unit": "GFLOP/s", "n_gpus": 1,
+        "metric": METRIC, "value": round(world * flops / (ms * 1e-3) / 1e9, 2), "unit": "GFLOP/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic N(0,1) complex with 1% of entries x1e3 (seeded)",
-        "config": {"workload": " + ".join(f"cfft1d f32 N={n} x {b}" for _, n, b in parts) + ", forward, plain FP32 path",
-                   "l2": "inputs larger than L2 (512 MiB per part)"},
-        "hbm_gbs": round(nbytes / (ms * 1e-3) / 1e9, 1),
-        "parts": {name: {"ms": round(t, 4), "gbs": round(16.0 * n * b / (t * 1e-3) / 1e9, 1),
-                         "frac_of_measured_hbm": round(16.0 * n * b / (t * 1e-3) / 1e9 / 6767.1, 4)}
-                  for (name, n, b), t in zip(parts, part_ms)},
-        "max_rel_l2_vs_fp64": worst,
-        "tensor_core_form": tc_parts,
+        "config": {"workload": PREC_WORKLOAD, "l2": "inputs larger than L2 (512 MiB per part), no flush",
+                   "parallelism": f"replicas x{world}", "path": "plain FP32 kernels (value); tensor cores in tc_vs_fp32"},
+        "hbm_gbs": round(world * nbytes / (ms * 1e-3) / 1e9, 1),
+        "parts_ms": {parts[i][0]: round(means[i], 4) for i in range(len(parts))},
+        "parts_frac_of_hbm": {parts[i][0]: round(16.0 * parts[i][1] * parts[i][2] / (means[i] * 1e-3) / 1e9 / peak, 4)
+                              for i in range(len(parts))},
+        "max_rel_l2_vs_fp64": max(fp32_err),
+        "roofline": {"bound": "hbm", "kernel": kernel, "part": dname, "achieved": round(achieved, 1), "peak": peak,
+                     "peak_source": f"{peak_src} hbm_gbs", "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": traffic, "traffic_note": "DRAM read + write bytes per launch (ncu, profiles/)",
+                     "algorithmic_bytes": dom_bytes},
+        "tc_vs_fp32": tc,
         "four_step_forms": forms,
-        "e2e": {"value": round(flops / e2e_s / 1e9, 2), "unit": "GFLOP/s",
-                "h2d_bytes_per_step": int(nbytes / 2), "d2h_bytes_per_step": int(nbytes / 2),
-                "ms_per_step": round(e2e_s * 1e3, 3)},
+        "e2e": {"value": round(world * flops / e2e_s / 1e9, 2), "unit": "GFLOP/s", "h2d_bytes_per_step": int(nbytes / 2),
+                "d2h_bytes_per_step": int(nbytes / 2), "ms_per_step": round(e2e_s * 1e3, 3)},
+        "gpu_launches": len(parts) * args.steps,
         "clocks": clk,
     }
+    if world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, t, desc = prec_cpu(parts, 2, threads)
+        line["cpu_baseline"] = {"value": round(v, 3), "unit": "GFLOP/s", "cores": threads, "kind": "port",
+                                "sample": f"{desc} (bounded sample), median of 2 after 1 warm-up, all host threads"}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -867,25 +975,24 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--pipe", default="2,4,1;4,8,1;3,6,0",
-                    help="large workload: pipelined four-step schedules to time (lead,ring,hints; ';'-separated)")
     ap.add_argument("--uneven-subset", default="all", choices=["all", "small", "big_c2c", "big_prime", "big_real"],
                     help="uneven workload: time one class of its jobs (profiling)")
     ap.add_argument("--small", action="store_true",
-                    help="large workload only: the same kernels at 1/4 and 1/2 the batch (profiling case)")
-    ap.add_argument("--workload", choices=["batch", "large", "uneven", "costmodel", "f64"], default="batch",
-                    help="batch: the headline configuration (default); large / uneven / costmodel / f64: the others")
+                    help="default workload only: the same kernels at 2^20 x 16 and 4096 x 4096 (profiling case)")
+    ap.add_argument("--workload", choices=["precision", "batch", "uneven", "costmodel", "f64"], default="precision",
+                    help="precision: 64 x 2^20 + 16384 x 4096 with the tensor-core comparison (default); "
+                         "batch / uneven / costmodel / f64: the other configurations")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
+        if args.workload == "precision":
+            return run_precision_reference(args, rank, world)
         return run_reference(args, rank, world)
     if args.workload == "uneven":
         return run_uneven(args)
-    if args.workload == "large":
-        return run_large(args)
     if args.workload == "costmodel":
         return run_costmodel(args)
     if args.workload == "f64":
@@ -895,6 +1002,8 @@ def main():
 
         torch.distributed.init_process_group("nccl")
     try:
+        if args.workload == "precision":
+            return run_precision(args, rank, world, local_rank)
         return run_gpu(args, rank, world, local_rank)
     finally:
         if world > 1:

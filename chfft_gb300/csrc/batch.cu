@@ -28,8 +28,7 @@
 namespace chfft {
 
 int record_error(int code, const std::string& msg);
-cudaError_t launch_batch(const BatchArgs& a, unsigned blocks, size_t smem, cudaStream_t stream, bool persist);
-int batch_blocks_per_sm(size_t smem);
+cudaError_t launch_batch(const BatchArgs& a, unsigned blocks, size_t smem, cudaStream_t stream);
 
 namespace {
 
@@ -207,7 +206,6 @@ struct BatchImpl {
   int ntasks = 0, nitems = 0, nctr = 0, nbig = 0;
   size_t smem = 0, work_bytes = 0;
   unsigned blocks = 0;  // CTAs per launch
-  bool persist = false;  // resident CTAs looping over the queue (else one CTA per task)
   cudaStream_t stream = nullptr;
   // captured launch
   cudaGraph_t graph = nullptr;
@@ -234,8 +232,11 @@ struct BatchImpl {
     a.in = static_cast<const char*>(d_in);
     a.out = static_cast<char*>(d_out);
     a.work = static_cast<char*>(d_work.p);
-    a.spin_limit = 10 * 1000 * 1000;  // x 200 ns: ~2 s before a wait gives up
-    CHFFT_CUDA(launch_batch(a, blocks, smem, s, persist));
+    // CHFFT_SPIN_LIMIT polls (default ~1 s); CHFFT_TEST_STALL=1 makes every
+    // dependency unreachable (the waits run out, chfft_batch_wait reports it).
+    a.spin_limit = (int)std::min<long long>(spin_limit(), 0x7fffffffLL);
+    a.stall = stall_test();
+    CHFFT_CUDA(launch_batch(a, blocks, smem, s));
   }
 };
 
@@ -468,14 +469,7 @@ int chfft_batch_create(int dtype, const chfft_batch_job* jobs, size_t njobs, chf
       CHFFT_CUDA(cudaMemcpyAsync(B.d_items.p, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice, s));
     if (!tasks.empty())
       CHFFT_CUDA(cudaMemcpyAsync(B.d_tasks.p, tasks.data(), tasks.size() * sizeof(BatchTask), cudaMemcpyHostToDevice, s));
-    int dev = 0, sms = 0;
-    CHFFT_CUDA(cudaGetDevice(&dev));
-    CHFFT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const int per_sm = batch_blocks_per_sm(smem);
-    const char* pe = std::getenv("CHFFT_BATCH_PERSISTENT");
-    B.persist = pe && *pe && std::strcmp(pe, "0") != 0;
-    B.blocks = B.persist ? (unsigned)std::max(1, std::min(per_sm * sms, std::max(1, B.ntasks)))
-                         : (unsigned)std::max(1, B.ntasks);
+    B.blocks = (unsigned)std::max(1, B.ntasks);
     CHFFT_CUDA(cudaStreamSynchronize(s));
   } catch (const Fail& f) {
     return record_error(f.code, f.msg);

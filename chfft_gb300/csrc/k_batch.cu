@@ -93,11 +93,16 @@ __device__ __forceinline__ void real_post(const BatchItem& it, char* out_base, i
   }
 }
 
+// Bounded wait of thread 0 for a dependency counter. After a time-out (or
+// once another task's wait timed out) the task goes on without its inputs;
+// the host reads the error word and reports CHFFT_ETIMEOUT. A.stall (test
+// hook) raises every target by one, so no dependency is ever met.
 __device__ __forceinline__ void wait_for(const BatchArgs& A, int ctr, int target) {
   if (threadIdx.x == 0) {
+    target += A.stall;
     int it = 0;
     while (ld_acquire(A.ctr + ctr) < target) {  // acquire: the producers' stores are visible after it
-      if (++it > A.spin_limit) {
+      if (++it > A.spin_limit || *(volatile int*)A.err) {
         atomicExch(A.err, 1);
         break;
       }
@@ -116,7 +121,6 @@ __device__ __forceinline__ void signal(const BatchArgs& A, int ctr) {
 }
 
 // One task of the queue, ticket ti (s_item: the CTA's descriptor copy).
-template <bool PERSIST>
 __device__ __forceinline__ void batch_task(const BatchArgs& A, int ti, unsigned char* smem_raw, BatchItem& s_item) {
   C* sbase = reinterpret_cast<C*>(smem_raw);
   const BatchTask tk = A.tasks[ti];
@@ -215,19 +219,12 @@ __device__ __forceinline__ void batch_task(const BatchArgs& A, int ti, unsigned 
     __syncthreads();
   };
   const bool two_rounds = core.blue || tk.type == BT_FS_BB;
-  if constexpr (PERSIST) {  // one call site inside the task loop
-    for (int r = 0; r < (two_rounds ? 2 : 1); r++) {
-      if (r == 1) between();
-      smem_passes<false, false, kBatchEpt>(core.st.all, m, 1, tpb, static_cast<const C*>(core.tw), sm);
-    }
-  } else {
-    // Two call sites rather than a loop over the rounds: a loop around the
-    // passes makes the compiler spill.
+  // Two call sites rather than a loop over the rounds: a loop around the
+  // passes makes the compiler spill.
+  smem_passes<false, false, kBatchEpt>(core.st.all, m, 1, tpb, static_cast<const C*>(core.tw), sm);
+  if (two_rounds) {
+    between();
     smem_passes<false, false, kBatchEpt>(core.st.all, m, 1, tpb, static_cast<const C*>(core.tw), sm);
-    if (two_rounds) {
-      between();
-      smem_passes<false, false, kBatchEpt>(core.st.all, m, 1, tpb, static_cast<const C*>(core.tw), sm);
-    }
   }
 
   // ---- store phase
@@ -322,12 +319,10 @@ __device__ __forceinline__ void batch_task(const BatchArgs& A, int ti, unsigned 
   if (tk.signal_ctr >= 0) signal(A, tk.signal_ctr);
 }
 
-// PERSIST: resident CTAs loop over the queue. Otherwise one CTA per task,
-// each taking its ticket when it starts: a task then only waits on tickets
-// taken earlier by running CTAs, as in the looping form. Without the loop
-// the compiler keeps the pass code in registers (the loop made it spill
-// 836 bytes per thread).
-template <bool PERSIST>
+// One CTA per task, each taking its ticket when it starts: a task then only
+// waits on tickets taken earlier by CTAs that are running, so no order of
+// residency can deadlock. (A loop of resident CTAs over the queue made the
+// compiler spill 836 bytes per thread around the pass code.)
 __global__ void __launch_bounds__(kBatchThreads, 2) k_batch(const BatchArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_task;
@@ -335,27 +330,16 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_batch(const BatchArgs A) {
   // all through the task, from shared memory instead of global memory.
   __shared__ __align__(16) BatchItem s_item;
   static_assert(sizeof(BatchItem) % 4 == 0, "item descriptor copied as 32-bit words");
-  if constexpr (PERSIST) {
-    for (;;) {
-      __syncthreads();
-      if (threadIdx.x == 0) s_task = atomicAdd(A.next, 1);
-      __syncthreads();
-      const int ti = s_task;
-      if (ti >= A.ntasks) return;
-      batch_task<true>(A, ti, smem_raw, s_item);
-    }
-  } else {
-    if (threadIdx.x == 0) s_task = atomicAdd(A.next, 1);
-    __syncthreads();
-    const int ti = s_task;
-    if (ti < A.ntasks) batch_task<false>(A, ti, smem_raw, s_item);
-  }
+  if (threadIdx.x == 0) s_task = atomicAdd(A.next, 1);
+  __syncthreads();
+  const int ti = s_task;
+  if (ti < A.ntasks) batch_task(A, ti, smem_raw, s_item);
 }
 
 }  // namespace
 
-cudaError_t launch_batch(const BatchArgs& a, unsigned blocks, size_t smem, cudaStream_t stream, bool persist) {
-  auto fn = persist ? k_batch<true> : k_batch<false>;
+cudaError_t launch_batch(const BatchArgs& a, unsigned blocks, size_t smem, cudaStream_t stream) {
+  auto fn = k_batch;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -364,11 +348,5 @@ cudaError_t launch_batch(const BatchArgs& a, unsigned blocks, size_t smem, cudaS
   return cudaGetLastError();
 }
 
-int batch_blocks_per_sm(size_t smem) {
-  int n = 0;
-  if (smem > 48 * 1024) cudaFuncSetAttribute(k_batch<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch<true>, kBatchThreads, smem) != cudaSuccess) return 1;
-  return n > 0 ? n : 1;
-}
 
 }  // namespace chfft

@@ -84,7 +84,8 @@ struct BatchArgs {
   const char* in;
   char* out;
   char* work;
-  int spin_limit;     // wait iterations before giving up
+  int spin_limit;     // wait iterations (~0.2 us apart) before giving up
+  int stall;          // test hook: 1 raises every dependency target by one (no wait is ever met)
 };
 
 constexpr int kPostChunk = 2048;  // pairs per POST task

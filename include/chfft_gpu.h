@@ -171,13 +171,15 @@ CHFFT_API int chfft_execute_device_noalloc(chfft_plan plan, int method, const vo
 /* ---- uneven batches ------------------------------------------------------ */
 
 /* Many transforms of mixed kinds and lengths in one launch fed by a device
- * work queue (CTAs take tasks by ticket: one task per CTA, or, with
- * CHFFT_BATCH_PERSISTENT=1 at create time, resident CTAs looping). No counterpart in the reference (one chfft call is one
+ * work queue (one CTA per task; each CTA takes its task by ticket when it
+ * starts). No counterpart in the reference (one chfft call is one
  * transform); each job means the reference call `plan.method(&src)` of its
  * kind at its length. Jobs are f32 forward methods of CFft1D, RFft1D, Dct1D
  * (DCT-II) and Mdct1D; lengths from 2 up to 2^18 (C2C) and a 7-smooth half
  * length for real kinds beyond 8192. Lengths beyond one CTA run as four-step
- * task chains synchronised by device counters (bounded waits). */
+ * task chains synchronised by device counters (bounded waits:
+ * CHFFT_SPIN_LIMIT polls, about a second by default; chfft_batch_wait
+ * reports a wait that gave up as CHFFT_ETIMEOUT). */
 typedef struct chfft_batch_job {
   int kind;          /* CHFFT_KIND_CFFT1D, _RFFT1D, _DCT1D (type II), _MDCT1D */
   int method;        /* a forward method of the kind (CHFFT_FORWARD, ...) */
