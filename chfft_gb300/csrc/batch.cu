@@ -183,7 +183,6 @@ bool build_big(HostBig& hb, long long n, bool blue_ok, cudaStream_t s) {
   hb.fs.n1 = n1;
   hb.fs.n2 = n2;
   hb.fs.tw_shift = sh;
-  hb.fs.l2_hints = 0;
   hb.fs.lo = hb.lo.p;
   hb.fs.hi = hb.hi.p;
   hb.fs.n_user = n;

@@ -340,16 +340,6 @@ int jit_launch(Kernel k, int dtype, const Core& c, const Geo& g0, const KArgs& a
   CUfunction fn = nullptr;
   const std::string expr = name_expression(k, dtype, c, *sp.sl, g, mode);
   if (int r = kernel_for(expr, g.smem, &fn)) return r;
-  // L2 prefetch of the next wave's input (rows, columns, four-step passes).
-  const bool prefetching = k == Kernel::C2C || k == Kernel::COLS || four_step(k);
-  a.ahead = 0;
-  if (prefetching && g.prefetch > 0) {
-    int per_sm = 0;
-    if (g_api.cuOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, g.threads, g.smem) == 0 && per_sm > 0) {
-      const long long resident = (long long)per_sm * num_sms();
-      if (g.prefetch > 0 || (long long)blocks > resident) a.ahead = resident;
-    }
-  }
   void* args[] = {const_cast<KArgs*>(&a), const_cast<FourStep*>(fs)};
   if (g_api.cuLaunchKernel(fn, blocks, 1, 1, g.threads, 1, 1, (unsigned)g.smem, (CUstream)stream, args, nullptr) != 0)
     return 2;

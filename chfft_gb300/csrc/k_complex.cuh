@@ -11,23 +11,6 @@ namespace chfft {
 
 namespace kern {
 
-// L2 prefetch of a later CTA's input. A launch of more CTAs than fit the GPU
-// at once runs in waves; the CTA that starts on an SM when this one retires
-// is about `ahead` (the CTAs resident at once) blocks later, so each CTA asks
-// L2 for that tile's input lines (128-byte lines spread over its threads)
-// and the next wave's HBM reads overlap this wave's passes.
-__device__ __forceinline__ void prefetch_l2(const void* p) {
-  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-}
-// `rows` runs of `bytes` bytes, `stride` bytes apart.
-__device__ __forceinline__ void prefetch_rows(const char* base, long long rows, long long bytes, long long stride) {
-  const long long lines = (bytes + 127) / 128;
-  for (long long i = threadIdx.x; i < rows * lines; i += blockDim.x) {
-    const long long r = i / lines, l = i - r * lines;
-    prefetch_l2(base + r * stride + l * 128);
-  }
-}
-
 // ---------------------------------------------------------------- rows
 // Contiguous sequences. The backward transform conjugates on the way in and
 // out (conj(F(conj x)) = F^-1 x up to scale), so one set of forward
@@ -63,12 +46,6 @@ __global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_c2c(cons
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
-  if (a.ahead > 0) {
-    const long long nx = (long long)blockIdx.x + a.ahead;
-    if (nx * a.tpb < a.count)
-      prefetch_rows((const char*)((const C*)a.in + nx * a.tpb * a.in_dist), min((long long)a.tpb, a.count - nx * a.tpb),
-                    (long long)a.core.n * sizeof(C), a.in_dist * (long long)sizeof(C));
-  }
   const long long t0 = (long long)blockIdx.x * a.tpb;
   const int nvalid = (int)min((long long)a.tpb, a.count - t0);
   RowLoad<C> ld{(const C*)a.in + t0 * a.in_dist, a.in_dist, nvalid, (T)a.scale, a.back};
@@ -108,15 +85,6 @@ __global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_cols(con
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
-  if (a.ahead > 0) {
-    const long long nx = (long long)blockIdx.x + a.ahead;
-    if (nx < a.count * a.tiles_per_tr) {
-      const long long ntr = nx / a.tiles_per_tr;
-      const int nc0 = (int)(nx - ntr * a.tiles_per_tr) * a.tpb;
-      prefetch_rows((const char*)((const C*)a.in + ntr * a.in_dist + nc0), a.core.n,
-                    (long long)min(a.tpb, a.ncols - nc0) * sizeof(C), (long long)a.ncols * sizeof(C));
-    }
-  }
   const long long tr = blockIdx.x / a.tiles_per_tr;
   const int c0 = (int)(blockIdx.x - tr * a.tiles_per_tr) * a.tpb;
   const int nvalid = min(a.tpb, a.ncols - c0);
@@ -133,11 +101,8 @@ __global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_cols(con
 // L a power of two so the split is a shift and a mask
 // (FourStep in kernels.cuh).
 
-// The four-step kernels' MODE template argument: bits 0-1 the pass mode,
-// bit 2 (kL2Hints) L2 eviction priorities: the intermediate is stored
-// evict_last so pass B can find it in L2, streamed data goes evict_first.
-constexpr int kL2Hints = 4;
-// Bit 3 (kSmemTwiddle): pass A builds, per CTA, the tables
+// The four-step kernels' MODE template argument: bits 0-1 the pass mode;
+// bit 3 (kSmemTwiddle): pass A builds, per CTA, the tables
 // A[t][q] = w_N^(32 q c) and B[t][r] = w_N^(r c) (c = c0 + t, q < ceil(N1 / 32),
 // r < 32) in shared memory after its tile, so the store's w_N^(k1 c) =
 // A[t][k1 / 32] B[t][k1 % 32] costs two shared loads instead of two global
@@ -146,18 +111,14 @@ constexpr int kSmemTwiddle = 8;
 
 // Pass A loader: MODE 0 plain (scale, conjugate for backward); MODE 1 the
 // Bluestein input x_j c_j for flat index j = n1 N2 + n2 < n_user, else 0.
-template <typename C, int MODE, bool HINTS>
+template <typename C, int MODE>
 struct ColsALoad {
   const C* in;  // first column of the tile
   int ncols, nvalid, c0;
   typename Real<C>::type scale;
   int back;
   const FourStep* fs;
-  unsigned long long pol;  // L2 policy of the streamed input (HINTS)
-  __device__ __forceinline__ C get(long long k) const {
-    if constexpr (HINTS) return ld_policy(in + k, pol);
-    return in[k];
-  }
+  __device__ __forceinline__ C get(long long k) const { return in[k]; }
   __device__ __forceinline__ C load(int t, int i) const {
     if (t >= nvalid) return czero<C>();
     if (MODE == 1) {
@@ -172,12 +133,11 @@ struct ColsALoad {
   }
 };
 
-template <typename C, bool HINTS, bool STWID = false>
+template <typename C, bool STWID = false>
 struct ColsAStore {
   C* out;
   int ncols, nvalid, c0;
   const FourStep* fs;
-  unsigned long long pol;  // L2 policy of the intermediate (HINTS)
   const C* tw;             // STWID: the per-CTA tables A (tpb x qa) then B (tpb x qb), rows padded
   int qa, qb, tpb;
   __device__ __forceinline__ void store(int t, int k1, C v) const {
@@ -191,10 +151,7 @@ struct ColsAStore {
       const C* hi = static_cast<const C*>(fs->hi);
       w = cmul(__ldg(&hi[e >> fs->tw_shift]), __ldg(&lo[e & ((1LL << fs->tw_shift) - 1)]));
     }
-    if constexpr (HINTS)
-      st_policy(out + (long long)k1 * ncols + t, cmul(v, w), pol);
-    else
-      out[(long long)k1 * ncols + t] = cmul(v, w);
+    out[(long long)k1 * ncols + t] = cmul(v, w);
   }
 };
 
@@ -206,12 +163,8 @@ __device__ __forceinline__ void cols_tw_tile(const KArgs& a, const FourStep& fs,
   using C = cx_t<T>;
   const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
   const int nvalid = min(a.tpb, a.ncols - c0);
-  // The input streams through L2 once; the intermediate should stay for pass B.
-  constexpr bool kHints = (MODE & kL2Hints) != 0;
-  const unsigned long long pin = kHints ? l2_evict_first() : 0ull;
-  const unsigned long long pout = kHints ? l2_evict_last() : 0ull;
-  ColsALoad<C, MODE & 3, kHints> ld{(const C*)a.in + tr_in * a.in_dist + c0, a.ncols, nvalid, c0, (T)a.scale,
-                                    a.back, &fs, pin};
+  ColsALoad<C, MODE & 3> ld{(const C*)a.in + tr_in * a.in_dist + c0, a.ncols, nvalid, c0, (T)a.scale, a.back,
+                            &fs};
   constexpr bool kStw = (MODE & kSmemTwiddle) != 0;
   C* twt = nullptr;
   const int qa = smem_twiddle_stride_a(fs.n1), qb = smem_twiddle_stride_b(a.tpb);
@@ -230,8 +183,7 @@ __device__ __forceinline__ void cols_tw_tile(const KArgs& a, const FourStep& fs,
       twt[i] = cmul(__ldg(&hi[e >> fs.tw_shift]), __ldg(&lo[e & mask]));
     }
   }
-  ColsAStore<C, kHints, kStw> st{(C*)a.out + tr_out * a.out_dist + c0, a.ncols, nvalid, c0, &fs, pout, twt, qa, qb,
-                                 a.tpb};
+  ColsAStore<C, kStw> st{(C*)a.out + tr_out * a.out_dist + c0, a.ncols, nvalid, c0, &fs, twt, qa, qb, a.tpb};
   CoreT::run(a.core, a.tpb, sm, ld, st);
 }
 
@@ -239,18 +191,6 @@ template <typename T, class CoreT, int MODE>
 __global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_cols_tw(const KArgs a, const FourStep fs) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  if (a.ahead > 0) {
-    const long long nx = (long long)blockIdx.x + a.ahead;
-    if (nx < a.count * a.tiles_per_tr) {
-      const long long ntr = nx / a.tiles_per_tr;
-      const int nc0 = (int)(nx - ntr * a.tiles_per_tr) * a.tpb;
-      // MODE 1 reads flat indices below n_user only (the rest is zero padding).
-      const long long rows =
-          (MODE & 3) == 1 ? min((long long)fs.n1, (fs.n_user - nc0 + a.ncols - 1) / a.ncols) : fs.n1;
-      prefetch_rows((const char*)((const C*)a.in + ntr * a.in_dist + nc0), rows,
-                    (long long)min(a.tpb, a.ncols - nc0) * sizeof(C), (long long)a.ncols * sizeof(C));
-    }
-  }
   const long long tr = blockIdx.x / a.tiles_per_tr;
   const int c0 = (int)(blockIdx.x - tr * a.tiles_per_tr) * a.tpb;
   cols_tw_tile<T, CoreT, MODE>(a, fs, tr, tr, c0, smem_raw);
@@ -261,18 +201,12 @@ __global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_cols_tw(
 // MODE 1 Bluestein spectrum: conj(X_k B^_k), the inverse FFT's input;
 // MODE 2 Bluestein output: k < n_user gets conj(X_k) c_k (conjugated again
 // for backward).
-template <typename C, int MODE, bool HINTS>
+template <typename C, int MODE>
 struct RowsBStore {
   C* out;  // transform base
   int r0, nvalid, n1, back;
   const FourStep* fs;
-  unsigned long long pol;  // L2 policy of the output (HINTS)
-  __device__ __forceinline__ void put(long long k, C v) const {
-    if constexpr (HINTS)
-      st_policy(out + k, v, pol);
-    else
-      out[k] = v;
-  }
+  __device__ __forceinline__ void put(long long k, C v) const { out[k] = v; }
   __device__ __forceinline__ void store(int t, int k2, C v) const {
     if (t >= nvalid) return;
     const long long k = (long long)(r0 + t) + (long long)n1 * k2;
@@ -289,16 +223,13 @@ struct RowsBStore {
   }
 };
 
-template <typename C, bool HINTS>
+template <typename C>
 struct RowsBLoad {
   const C* in;  // first row of the tile
   int n2, nvalid;
-  unsigned long long pol;  // the intermediate is read once more, then dropped first (HINTS)
   __device__ __forceinline__ C load(int t, int i) const {
     if (t >= nvalid) return czero<C>();
-    const long long k = (long long)t * n2 + i;
-    if constexpr (HINTS) return ld_policy(in + k, pol);
-    return in[k];
+    return in[(long long)t * n2 + i];
   }
 };
 
@@ -314,12 +245,8 @@ __device__ __forceinline__ void rows_t_tile(const KArgs& a, const FourStep& fs, 
   // then run the FFT with consecutive threads across rows so the transposed
   // store is contiguous. Compile-time-stage cores fuse the row load into
   // their first pass; the others stage it through the tile.
-  // MODE 1 writes the next pass's input (kept in L2); otherwise the output streams out.
-  constexpr bool kHints = (MODE & kL2Hints) != 0;
-  const unsigned long long pin = kHints ? l2_evict_first() : 0ull;
-  const unsigned long long pout = kHints ? ((MODE & 3) == 1 ? l2_evict_last() : l2_evict_first()) : 0ull;
-  RowsBLoad<C, kHints> rl{(const C*)a.in + tr_in * a.in_dist + (long long)r0 * fs.n2, fs.n2, nvalid, pin};
-  RowsBStore<C, MODE & 3, kHints> st{(C*)a.out + tr_out * a.out_dist, r0, nvalid, fs.n1, a.back, &fs, pout};
+  RowsBLoad<C> rl{(const C*)a.in + tr_in * a.in_dist + (long long)r0 * fs.n2, fs.n2, nvalid};
+  RowsBStore<C, MODE & 3> st{(C*)a.out + tr_out * a.out_dist, r0, nvalid, fs.n1, a.back, &fs};
   if constexpr (CoreT::kStatic) {
     CoreT::template run<true>(a.core, a.tpb, sm, rl, st);
   } else {
@@ -332,15 +259,6 @@ template <typename T, class CoreT, int MODE>
 __global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_rows_t(const KArgs a, const FourStep fs) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  if (a.ahead > 0) {
-    const long long nx = (long long)blockIdx.x + a.ahead;
-    if (nx < a.count * a.tiles_per_tr) {
-      const long long ntr = nx / a.tiles_per_tr;
-      const int nr0 = (int)(nx - ntr * a.tiles_per_tr) * a.tpb;
-      prefetch_rows((const char*)((const C*)a.in + ntr * a.in_dist + (long long)nr0 * fs.n2), 1,
-                    (long long)min(a.tpb, fs.n1 - nr0) * fs.n2 * sizeof(C), 0);
-    }
-  }
   const long long tr = blockIdx.x / a.tiles_per_tr;
   const int r0 = (int)(blockIdx.x - tr * a.tiles_per_tr) * a.tpb;
   rows_t_tile<T, CoreT, MODE>(a, fs, tr, tr, r0, smem_raw);
@@ -368,12 +286,11 @@ struct RowSpectrumStore {
   }
 };
 
-template <typename C, bool HINTS>
+template <typename C>
 struct RowsBBStore {
   C* out;  // the transform's n2 x n1 intermediate
   int r0, nvalid, n1;
   const FourStep* fs;
-  unsigned long long pol;
   __device__ __forceinline__ void store(int t, int m2, C v) const {
     if (t >= nvalid) return;
     const int k1 = r0 + t;
@@ -382,10 +299,7 @@ struct RowsBBStore {
     const C* hi = static_cast<const C*>(fs->hi);
     const C w = cmul(__ldg(&hi[e >> fs->tw_shift]), __ldg(&lo[e & ((1LL << fs->tw_shift) - 1)]));
     const long long k = k1 + (long long)n1 * m2;
-    if constexpr (HINTS)
-      st_policy(out + k, cmul(v, w), pol);
-    else
-      out[k] = cmul(v, w);
+    out[k] = cmul(v, w);
   }
 };
 
@@ -397,12 +311,9 @@ __global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_rows_bb(
   const long long tr = blockIdx.x / a.tiles_per_tr;
   const int r0 = (int)(blockIdx.x - tr * a.tiles_per_tr) * a.tpb;
   const int nvalid = min(a.tpb, fs.n1 - r0);
-  constexpr bool kHints = (MODE & kL2Hints) != 0;
-  const unsigned long long pin = kHints ? l2_evict_first() : 0ull;
-  const unsigned long long pout = kHints ? l2_evict_last() : 0ull;
-  RowsBLoad<C, kHints> rl{(const C*)a.in + tr * a.in_dist + (long long)r0 * fs.n2, fs.n2, nvalid, pin};
+  RowsBLoad<C> rl{(const C*)a.in + tr * a.in_dist + (long long)r0 * fs.n2, fs.n2, nvalid};
   RowSpectrumStore<C, decltype(sm)> spec{sm, static_cast<const C*>(fs.bhat), r0, fs.n1};
-  RowsBBStore<C, kHints> st{(C*)a.out + tr * a.out_dist, r0, nvalid, fs.n1, &fs, pout};
+  RowsBBStore<C> st{(C*)a.out + tr * a.out_dist, r0, nvalid, fs.n1, &fs};
   if constexpr (CoreT::kStatic) {
     CoreT::template run<true>(a.core, a.tpb, sm, rl, spec);
     CoreT::template run<false>(a.core, a.tpb, sm, sm, st);

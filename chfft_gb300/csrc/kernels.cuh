@@ -30,7 +30,6 @@ struct KArgs {
   const void* aux1;        // second table (omega_4N, window)
   double aux_scalar;       // kind constant (DCT ortho factor)
   int* err;                // device error word, may be null
-  long long ahead;         // > 0: prefetch into L2 the input of the CTA this many blocks later
 };
 
 enum class Kernel : int {
@@ -57,7 +56,6 @@ struct FourStep {
   long long n_user;   // Bluestein: user length (inputs past it are zero, outputs dropped)
   const void* chirp;  // Bluestein: c_j, j < n_user
   const void* bhat;   // Bluestein: FFT_N(conj c) / N
-  int l2_hints;       // host side: the plan-time kernels run with L2 eviction priorities (mode bit 2)
 };
 
 // Pass A's per-CTA twiddle tables: tpb rows of ceil(n1 / 32) entries, then
@@ -71,39 +69,11 @@ __host__ __device__ constexpr int smem_twiddle_entries(int tpb, int n1) {
   return tpb * (smem_twiddle_stride_a(n1) + smem_twiddle_stride_b(tpb));
 }
 
-// Global accesses with an L2 eviction-priority policy (createpolicy).
-__device__ __forceinline__ unsigned long long l2_evict_first() {
-  unsigned long long p;
-  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ unsigned long long l2_evict_last() {
-  unsigned long long p;
-  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ float2 ld_policy(const float2* p, unsigned long long pol) {
-  float2 v;
-  asm volatile("ld.global.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(p), "l"(pol));
-  return v;
-}
-__device__ __forceinline__ double2 ld_policy(const double2* p, unsigned long long pol) {
-  double2 v;
-  asm volatile("ld.global.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(v.x), "=d"(v.y) : "l"(p), "l"(pol));
-  return v;
-}
 // GPU-scope acquire load of a dependency counter.
 __device__ __forceinline__ int ld_acquire(const int* p) {
   int v;
   asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
-}
-
-__device__ __forceinline__ void st_policy(float2* p, float2 v, unsigned long long pol) {
-  asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(p), "f"(v.x), "f"(v.y), "l"(pol) : "memory");
-}
-__device__ __forceinline__ void st_policy(double2* p, double2 v, unsigned long long pol) {
-  asm volatile("st.global.L2::cache_hint.v2.f64 [%0], {%1, %2}, %3;" ::"l"(p), "d"(v.x), "d"(v.y), "l"(pol) : "memory");
 }
 
 #ifndef __CUDACC_RTC__

@@ -334,7 +334,6 @@ Geo row_geo(const Core& c, long long count, const PlanOpts& o) {
   g.max_radix = o.max_radix == 16 ? 16 : 32;
   g.min_blocks = o.min_blocks;
   g.balance = o.balance;
-  g.prefetch = o.prefetch;
   const int ept = ept_of(c.dtype);
   const int m = c.st.n;
   g.ld = smem_ld(m);
@@ -371,7 +370,6 @@ Geo col_geo(const Core& c, int ncols, int tpb_opt, const PlanOpts& o) {
   g.max_radix = o.max_radix == 16 ? 16 : 32;
   g.min_blocks = o.min_blocks;
   g.balance = o.balance;
-  g.prefetch = o.prefetch;
   // Elements per thread of the several-butterflies variant: the dtype's
   // default, or the `ept` knob (specialised kernels; a library kernel keeps
   // its own and leaves the extra threads idle).
@@ -433,8 +431,8 @@ bool four_step_split(long long m, int dtype, int* n1, int* n2) {
 
 static void launch_pass(bool pass_a, int mode, const Core& c, const Geo& g, const KArgs& a, const FourStep& fs,
                         unsigned blocks, long long elems, cudaStream_t s, bool library_only, int jit_opt, int tc) {
-  // Plan-time kernels carry the L2-priority choice in the mode's bit 2.
-  const int jmode = mode | (fs.l2_hints ? 4 : 0) | (pass_a && tc <= 0 ? 8 : 0);
+  // Plan-time pass-A kernels build their twiddle tables in shared memory (mode bit 3).
+  const int jmode = mode | (pass_a && tc <= 0 ? 8 : 0);
   if (tc > 0 && !library_only) {
     const int r = jit_launch_tc(pass_a ? Kernel::COLS_TW : Kernel::ROWS_T, c, tc, g.tpb, a, blocks, s, jmode, &fs);
     if (r == 2) throw Fail{CHFFT_ECUDA, "launch of a tensor-core kernel failed"};
@@ -552,7 +550,6 @@ FourStep BigCore::fs() const {
   f.lo = lo.p;
   f.hi = hi.p;
   f.n_user = n;
-  f.l2_hints = opts.l2_hints > 0 ? 1 : 0;
   f.chirp = chirp.p;
   f.bhat = bhat.p;
   return f;

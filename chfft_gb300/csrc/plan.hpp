@@ -100,8 +100,6 @@ struct PlanOpts {
   int min_blocks = 0;    // specialised kernels: launch-bounds CTAs per SM, 0 auto
   int balance = -1;      // specialised kernels: balanced mixed-radix variant (-1 auto = on, 0 off, 1 on)
   int ept = 0;           // column kernels: elements per thread of the several-butterflies variant, 0 default
-  int prefetch = -1;     // specialised row / column kernels: L2 prefetch of the next wave (1 on; -1 auto = off, 0 off)
-  int l2_hints = -1;     // four-step passes: L2 eviction priorities (intermediate kept, streams first) (1 on; -1 auto = off)
 };
 
 // Complex core FFT of logical length n for one dtype: mixed radix when n is
@@ -137,7 +135,6 @@ struct Geo {
   int min_blocks = 0;  // compile-time-stage kernels: launch-bounds CTAs per SM (0: 2 for k1, else 1)
   int ept = 0;         // compile-time-stage kernels: elements per thread of the several-butterflies variant
   int balance = -1;    // compile-time-stage kernels: balanced variant of a mixed-radix k1 geometry (-1 auto, 0 off)
-  int prefetch = -1;   // compile-time-stage row / column kernels: L2 prefetch of the next wave (1 on, else off)
 };
 Geo row_geo(const Core& c, long long count, const PlanOpts& o = PlanOpts{});
 Geo col_geo(const Core& c, int ncols, int tpb_opt = 0, const PlanOpts& o = PlanOpts{});

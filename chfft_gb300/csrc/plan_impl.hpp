@@ -365,37 +365,11 @@ struct PlanImpl {
   // chunk k+1, the transforms of chunk k and the copy-out of chunk k-1
   // overlap (copy engines of both directions and the SMs); with pinned host
   // memory the end-to-end time approaches the larger of the two copies.
-  // Device address of page-locked host memory mapped into the GPU's address
-  // space (cudaHostAlloc / cudaHostRegister), else null.
-  static const void* mapped(const void* p) {
-    cudaPointerAttributes at{};
-    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-      cudaGetLastError();
-      return nullptr;
-    }
-    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
-  }
-
   void exec_host(const MethodSpec& ms, const void* src, void* dst, long long batch) {
     cudaStream_t s = host_stream();
     const size_t ib1 = in_elems(ms.back) * in_esize(ms.back), ob1 = out_elems(ms.back) * out_esize(ms.back);
     const size_t ib = ib1 * batch, ob = ob1 * batch;
     if (ib == 0 && ob == 0) return;
-    // CHFFT_ZERO_COPY=1 with mapped page-locked buffers on both sides: the
-    // kernels read and write host memory directly over the CPU-GPU link, no
-    // staging copies. Off by default: on the headline workload it measured
-    // 1.30 ms end to end against 1.02 ms for the staged pipeline below.
-    const char* zc = std::getenv("CHFFT_ZERO_COPY");
-    if (zc && zc[0] == '1') {
-      const void* ms_src = mapped(src);
-      void* ms_dst = const_cast<void*>(mapped(dst));
-      if (ms_src && ms_dst) {
-        exec(ms, ms_src, ms_dst, batch, s);
-        CHFFT_CUDA(cudaStreamSynchronize(s));
-        check_waits();
-        return;
-      }
-    }
     stage_in.ensure(ib);
     stage_out.ensure(ob);
     const long long chunks =

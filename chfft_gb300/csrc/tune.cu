@@ -30,8 +30,6 @@ PlanOpts to_opts(const chfft_plan_config& c) {
   o.tc = c.tc_precision;
   o.min_blocks = c.min_blocks_per_sm;
   o.balance = c.balanced;
-  o.prefetch = c.l2_prefetch;
-  o.l2_hints = c.l2_evict_hints;
   o.ept = c.col_elems_per_thread;
   return o;
 }
@@ -49,8 +47,8 @@ chfft_plan_config to_cfg(const PlanOpts& o) {
   c.tc_precision = o.tc;
   c.min_blocks_per_sm = o.min_blocks;
   c.balanced = o.balance;
-  c.l2_prefetch = o.prefetch;
-  c.l2_evict_hints = o.l2_hints;
+  c.l2_prefetch = 0;     // retired knobs: always reported off
+  c.l2_evict_hints = 0;
   c.col_elems_per_thread = o.ept;
   return c;
 }
@@ -84,7 +82,7 @@ struct Resolved {
   int npass = 0, rfirst = 0, rlast = 0;
   int minb = 0;          // specialised kernels: launch-bounds CTAs per SM
   bool balanced = false;  // specialised kernels: balanced mixed-radix variant
-  int prefetch = 0;       // specialised kernels: next-wave L2 prefetch knob (-1 auto, 0 off, 1 on)
+  int prefetch = 0;       // retired next-wave L2 prefetch knob: always 0 (feature slot kept)
 
   auto key() const {
     return std::make_tuple(big, blue, k1, jit, wide, tpb, tile, n1, fft_len, l2mb, chunks, minb, balanced, prefetch);
@@ -215,7 +213,6 @@ Resolved resolve(const PlanImpl& p, long long batch, const PlanOpts& o) {
       one_cta(p.core.st, batch);
       break;
   }
-  r.prefetch = r.jit ? o.prefetch : 0;
   return r;
 }
 
@@ -334,9 +331,6 @@ std::vector<PlanOpts> candidates(const PlanImpl& p, long long batch, bool tune_j
           out.push_back(q);
           q = o;
           q.balance = 0;
-          out.push_back(q);
-          q = o;
-          q.prefetch = 1;
           out.push_back(q);
         }
       }

@@ -255,13 +255,10 @@ typedef struct chfft_plan_config {
   int balanced;            /* plan-time kernels with mixed radices: 1 / -1 (auto) every thread
                               takes maxR / R butterflies of a radix-R pass, 0 one butterfly per
                               thread and pass (threads idle through the larger radices) */
-  int l2_prefetch;         /* plan-time row / column / four-step kernels: 1 every CTA asks L2 for
-                              the input of the CTA one wave later (the next wave's HBM reads
-                              overlap this wave's passes), 0 / -1 (auto) off: measured slower on
-                              the configurations timed so far, kept as a tuning knob */
-  int l2_evict_hints;      /* four-step passes: 1 the intermediate is stored with an L2
-                              evict_last policy and the streamed input / output with
-                              evict_first; 0 / -1 (auto) plain accesses */
+  int l2_prefetch;         /* retired (next-wave L2 prefetch measured slower everywhere): ignored,
+                              always reported 0; kept so the struct layout does not change */
+  int l2_evict_hints;      /* retired (L2 eviction priorities on the two-launch four-step passes,
+                              superseded by the pipelined launch's own hints): ignored, reported 0 */
   int col_elems_per_thread; /* column / four-step kernels of the several-butterflies variant:
                                complex elements a thread holds (16 or 32), 0 the dtype's
                                default (32 f32, 16 f64) */
