@@ -424,8 +424,9 @@ size_t chfft_plan_compiler_cache_size(void) { return chfft::jit_cache_size(); }
 
 namespace chfft {
 
-// Sets the message chfft_last_error returns on this thread (noalloc.cu).
+// Sets / clears the message chfft_last_error returns on this thread (noalloc.cu).
 int record_error(int code, const std::string& msg) { return set_error(code, msg); }
+void clear_error() { tl_error.clear(); }
 
 // For the no-allocation entry point (noalloc.cu): the four-step core of a
 // CFft1D plan and the direction / scale of `method`. Returns a status and

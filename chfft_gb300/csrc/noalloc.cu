@@ -11,7 +11,9 @@
 // library holds until the process exits.
 #include <cuda_runtime.h>
 
+#include <exception>
 #include <mutex>
+#include <new>
 #include <string>
 
 #include "../../include/chfft_gpu.h"
@@ -21,6 +23,7 @@ namespace chfft {
 
 int plan_four_step(chfft_plan plan, int method, const BigCore** big, bool* back, double* scale);
 int record_error(int code, const std::string& msg);
+void clear_error();
 
 namespace {
 
@@ -29,24 +32,48 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[CHFFT_NOALLOC_S
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
+// Per device: the scratch's device address and the context it was looked
+// up in (a device reset makes a new context, and the address is looked up
+// again there).
 void* g_scratch_ptr[kMaxDevices] = {};
+void* g_scratch_ctx[kMaxDevices] = {};
 
 int fail(int code, const std::string& msg) { return record_error(code, msg); }
 
+// The driver's cuCtxGetCurrent, or null when it cannot be had.
+typedef int (*CtxGetCurrent)(void**);
+CtxGetCurrent ctx_getter() {
+  static std::once_flag once;
+  static CtxGetCurrent fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<CtxGetCurrent>(p);
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
 // Device address of the scratch on the current device, looked up once per
-// device (host code only sees a stand-in for the array's name).
+// device and context (host code only sees a stand-in for the array's name).
 int scratch_address(void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return fail(CHFFT_ECUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return fail(CHFFT_EUNSUPPORTED, "device ordinal out of range");
+  void* ctx = nullptr;
+  if (CtxGetCurrent get = ctx_getter()) get(&ctx);
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch_ptr[dev]) {
+  if (!g_scratch_ptr[dev] || g_scratch_ctx[dev] != ctx) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p)
       return fail(CHFFT_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
     g_scratch_ptr[dev] = p;
+    g_scratch_ctx[dev] = ctx;
   }
   *out = g_scratch_ptr[dev];
   return CHFFT_OK;
@@ -58,6 +85,7 @@ int scratch_address(void** out) {
 extern "C" int chfft_execute_device_noalloc(chfft_plan plan, int method, const void* d_src, void* d_dst,
                                             size_t batch, void* stream) {
   using namespace chfft;
+  clear_error();
   const BigCore* big = nullptr;
   bool back = false;
   double scale = 1.0;
@@ -81,6 +109,10 @@ extern "C" int chfft_execute_device_noalloc(chfft_plan plan, int method, const v
               (long long)((size_t)CHFFT_NOALLOC_SCRATCH_BYTES / per), /*library_only=*/true);
   } catch (const Fail& f) {
     return fail(f.code, f.msg);
+  } catch (const std::bad_alloc&) {
+    return fail(CHFFT_ENOMEM, "host allocation failed");
+  } catch (const std::exception& x) {
+    return fail(CHFFT_EINVAL, x.what());
   }
   return CHFFT_OK;
 }

@@ -163,7 +163,9 @@ CHFFT_API int chfft_plan_wait(chfft_plan plan, void* stream);
  * make that first call before any stream capture. All calls share the array
  * and it keeps the last call's contents (nothing in it needs to start at
  * zero), so calls whose work overlaps on the GPU (different streams, no
- * ordering) race on it. Other plans get CHFFT_EINVAL. */
+ * ordering) race on it. A device reset (cudaDeviceReset) discards the array's
+ * contents with the context; the next call looks the address up again in the
+ * new context. Other plans get CHFFT_EINVAL. */
 #define CHFFT_NOALLOC_SCRATCH_BYTES (16u << 20)
 CHFFT_API int chfft_execute_device_noalloc(chfft_plan plan, int method, const void* d_src, void* d_dst, size_t batch,
                                            void* stream);

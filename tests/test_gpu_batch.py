@@ -6,6 +6,8 @@ f64 oracle). Covers one-CTA jobs (mixed radix and Bluestein), four-step jobs
 (C2C, four-step Bluestein, R2C / DCT-II with a four-step half length and
 their post tasks), the CUDA-graph replay, and the bounded-wait status.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -105,3 +107,58 @@ def test_batch_rejects_bad_jobs():
         cg.Batch([("rfft1d", 33, "forward", 0)])
     with pytest.raises(cg.ChfftError):
         cg.Batch([("cfft1d", 64, "backward", 0)])
+
+
+def test_batch_full_uneven_workload():
+    """The whole 10,000-job uneven workload of the benchmark (lengths
+    log-uniform in [16, 65536], 15% prime, 60/20/10/10 C2C / R2C / DCT-II /
+    MDCT): every job against the oracle at 5e-6."""
+    import concurrent.futures as cf
+
+    import bench
+
+    specs = bench.uneven_specs()
+    b = cg.Batch(specs)
+    host_in, xs = make_inputs(specs, b, seed=9)
+    d_in = torch.from_numpy(host_in).cuda()
+    d_out = torch.zeros(max(b.out_bytes, 16), dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    b.execute(d_in.data_ptr(), d_out.data_ptr(), stream, graph=True)
+    b.wait(stream)
+    host_out = d_out.cpu().numpy()
+
+    def check(i):
+        kind, n, method, option = specs[i]
+        got = out_view(kind, n, host_out[b.offsets[i][1]:])
+        return rel(got, expected(kind, n, method, option, xs[i])), i
+
+    with cf.ThreadPoolExecutor(os.cpu_count() or 4) as ex:
+        worst, i = max(ex.map(check, range(len(specs))))
+    assert worst <= 5e-6, (specs[i], worst)
+
+
+def test_batch_bounded_wait_runs_out_and_recovers(monkeypatch):
+    """Every dependency unreachable (CHFFT_TEST_STALL=1, short
+    CHFFT_SPIN_LIMIT): the four-step tasks' waits give up, the launch
+    returns, chfft_batch_wait reports CHFFT_ETIMEOUT; the next launch of the
+    same batch on the same GPU is correct."""
+    specs = [("cfft1d", 65536, "forward", 0), ("cfft1d", 1000, "forward", 0), ("rfft1d", 40000, "forward", 0)]
+    b = cg.Batch(specs)
+    host_in, xs = make_inputs(specs, b)
+    d_in = torch.from_numpy(host_in).cuda()
+    d_out = torch.zeros(max(b.out_bytes, 16), dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    monkeypatch.setenv("CHFFT_TEST_STALL", "1")
+    monkeypatch.setenv("CHFFT_SPIN_LIMIT", "20000")
+    b.execute(d_in.data_ptr(), d_out.data_ptr(), stream)
+    with pytest.raises(cg.ChfftError) as e:
+        b.wait(stream)
+    assert e.value.status == cg.ETIMEOUT
+    monkeypatch.delenv("CHFFT_TEST_STALL")
+    monkeypatch.delenv("CHFFT_SPIN_LIMIT")
+    d_out.zero_()
+    b.execute(d_in.data_ptr(), d_out.data_ptr(), stream)
+    b.wait(stream)
+    host_out = d_out.cpu().numpy()
+    for (kind, n, method, option), (_, oo), x in zip(specs, b.offsets, xs):
+        assert rel(out_view(kind, n, host_out[oo:]), expected(kind, n, method, option, x)) <= 5e-6

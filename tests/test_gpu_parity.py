@@ -298,3 +298,30 @@ def test_config_1m_x64_f32():
     y = p.execute_batch("forward", x)
     for i in (0, 31, 63):
         assert rel(y[i], np.fft.fft(x[i].astype(np.complex128))) <= 1e-6
+
+
+# ---------------------------------------------------------------- index work on the GPU
+@pytest.mark.parametrize("n", [1009, 20011, 65521, 65537, 99991, 1000003])
+def test_chirp_index_device_bit_exact(n):
+    """chfft_chirp_index_device: (i*i) % 2N for i < N (src/cfft1d.rs:123-128),
+    bit for bit against the oracle; N = 65537 and above overflow 32 bits."""
+    torch = pytest.importorskip("torch")
+    d = torch.zeros(n, dtype=torch.int64, device="cuda")
+    cg.chirp_index_device(n, d.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(d.cpu().numpy().view(np.uint64), oracle.chirp_index(n))
+
+
+def test_config_4096x16384_fp32_outliers_every_row():
+    """N = 4096 x 16384 f32, N(0,1) with 1% of entries x 1e3: every row
+    within 1e-6 rel-L2 of numpy's FP64 FFT (the precision configuration)."""
+    n, b = 4096, 16384
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal((b, n), dtype=np.float32) + 1j * rng.standard_normal((b, n), dtype=np.float32)
+    x[rng.random((b, n)) < 0.01] *= 1e3
+    x = x.astype(np.complex64)
+    y = cg.CFft1D.with_len(n, np.float32).execute_batch("forward", x)
+    for lo in range(0, b, 2048):
+        ref = np.fft.fft(x[lo:lo + 2048].astype(np.complex128), axis=-1)
+        err = np.linalg.norm(y[lo:lo + 2048] - ref, axis=-1) / np.linalg.norm(ref, axis=-1)
+        assert err.max() <= 1e-6, (lo, float(err.max()))

@@ -154,9 +154,9 @@ def test_model_save_load_and_propose(tmp_path):
 def test_learned_plans_against_exhaustive_small(monkeypatch):
     """A small instance of the learned-plan protocol: timings of every
     candidate for seeded training lengths, a GPU-trained model, then held-out
-    lengths: the model's picks must stay within 15% of the exhaustive best on
-    (geometric) average and the run reports what the model gains over the
-    heuristic plan. Library kernels only (no plan-time compiles)."""
+    lengths: the model's picks must stay within 10% of the exhaustive best on
+    (geometric) average and beat the heuristic plan (the method without the
+    network). Library kernels only (no plan-time compiles)."""
     monkeypatch.setenv("CHFFT_JIT", "0")
     rng = np.random.default_rng(2024)
     train_len = tuning.log_uniform_lengths(rng, 48, 64, 1 << 18)
@@ -171,4 +171,5 @@ def test_learned_plans_against_exhaustive_small(monkeypatch):
     g_pick = float(np.exp(np.mean(np.log(pick))))
     g_heur = float(np.exp(np.mean(np.log(heur))))
     print(f"held-out: model {g_pick:.3f}x of exhaustive, heuristic {g_heur:.3f}x ({len(te)} cases)")
-    assert g_pick <= 1.15
+    assert g_pick <= 1.10  # within 10% of exhaustive autotuning
+    assert g_pick < g_heur  # the trained network beats the plan chosen without it

@@ -1,4 +1,4 @@
-"""chfft_execute_device_noalloc against chfft_execute_device.
+"""chfft_execute_device_noalloc against chfft_execute_device and numpy's FP64 FFT.
 
 The no-allocation entry point serves callers that cannot allocate device
 memory when a transform runs (stream capture, real-time loops, pooled
@@ -47,6 +47,9 @@ def test_noalloc_matches_execute_device(n, dt, batch):
     d_out = torch.empty_like(d_in)
     assert d_in.dtype == rdt
     stream = torch.cuda.current_stream().cuda_stream
+    xd = x.astype(np.complex128)
+    fp64 = {"forward": np.fft.fft(xd, axis=-1), "backwardu": np.fft.ifft(xd, axis=-1) * np.sqrt(n)}
+    ftol = 5e-6 if dt == np.float32 else 1e-11
     for method in ("forward", "backwardu"):
         p.execute_device(method, d_in.data_ptr(), d_ref.data_ptr(), batch, stream)
         ref = d_ref.cpu().numpy().view(cdt)
@@ -56,6 +59,7 @@ def test_noalloc_matches_execute_device(n, dt, batch):
             assert rc == 0, cg.lib().chfft_last_error().decode()
             out = d_out.cpu().numpy().view(cdt)
             assert rel(out, ref) <= tol, (method, call)
+            assert rel(out, fp64[method]) <= ftol, (method, call)  # independent FP64 check
 
 
 def test_noalloc_rejects_oversized_and_small_plans():
