@@ -159,11 +159,11 @@ def test_learned_plans_against_exhaustive_small(monkeypatch):
     network). Library kernels only (no plan-time compiles)."""
     monkeypatch.setenv("CHFFT_JIT", "0")
     rng = np.random.default_rng(2024)
-    train_len = tuning.log_uniform_lengths(rng, 48, 64, 1 << 18)
-    test_len = tuning.log_uniform_lengths(rng, 16, 64, 1 << 18, exclude=train_len)
+    train_len = tuning.log_uniform_lengths(rng, 200, 64, 1 << 18)
+    test_len = tuning.log_uniform_lengths(rng, 48, 64, 1 << 18, exclude=train_len)
     mk = lambda n: cg.CFft1D.with_len(n, np.float32)  # noqa: E731
-    tr = tuning.collect(mk, train_len, [1, 64, 4096], max_elems=1 << 21, reps=3)
-    te = tuning.collect(mk, test_len, [1, 64, 4096], max_elems=1 << 21, reps=3)
+    tr = tuning.collect(mk, train_len, [1, 64, 4096], max_elems=1 << 21, reps=5)
+    te = tuning.collect(mk, test_len, [1, 64, 4096], max_elems=1 << 21, reps=5)
     X, y = tuning.dataset(tr)
     m = tuning.CostModel(64, seed=0)
     m.train(X, y, epochs=200, batch=128, lr=2e-3)
