@@ -257,8 +257,9 @@ int chfft_plan_get_info(chfft_plan plan, chfft_plan_info* info) {
   info->len_m = (size_t)p.len_m;
   info->len_n = (size_t)p.len_n;
   info->fft_len = (size_t)(p.use_big ? p.big.n : p.core.n);
-  info->algorithm = p.use_big ? (p.big.blue ? 3 : 2) : (p.core.blue ? 1 : 0);
-  info->padded_len = p.use_big ? (p.big.blue ? (size_t)p.big.m : 0) : (p.core.blue ? (size_t)p.core.st.n : 0);
+  info->algorithm = p.use_big ? (p.big.blue ? 3 : 2) : p.use_rader ? 4 : (p.core.blue ? 1 : 0);
+  info->padded_len = p.use_big ? (p.big.blue ? (size_t)p.big.m : 0)
+                               : p.use_rader ? 0 : (p.core.blue ? (size_t)p.core.st.n : 0);
   int k = 0;
   if (p.core.st.npass >= 2) {
     info->radix[k++] = p.core.st.rf;
@@ -279,7 +280,7 @@ int chfft_plan_get_info(chfft_plan plan, chfft_plan_info* info) {
   info->in_elems = p.in_elems(false);
   info->out_elems = p.out_elems(false);
   info->device_bytes = p.core.device_bytes() + p.core2.device_bytes() + p.big.device_bytes() + p.work.bytes +
-                       p.aux0.bytes + p.aux1.bytes;
+                       p.aux0.bytes + p.aux1.bytes + p.rader.device_bytes();
   return CHFFT_OK;
 }
 

@@ -123,6 +123,7 @@ const char* kernel_template(Kernel k) {
     case Kernel::COLS_TW: return "chfft::kern::k_cols_tw";
     case Kernel::ROWS_T: return "chfft::kern::k_rows_t";
     case Kernel::ROWS_BB: return "chfft::kern::k_rows_bb";
+    case Kernel::C2C_RADER: return "chfft::kern::k_c2c_rader";
   }
   return "";
 }
@@ -285,6 +286,8 @@ bool resolve(Kernel k, int dtype, const Core& c, const Geo& g0, const KArgs& a0,
   g.smem = (size_t)g.tpb * g.ld * cplx_bytes(dtype);
   if (k == Kernel::COLS_TW && (mode & 8) && fs)  // pass A's twiddle tables after the tile
     g.smem = (g.smem + 15) / 16 * 16 + (size_t)smem_twiddle_entries(g.tpb, fs->n1) * cplx_bytes(dtype);
+  if (k == Kernel::C2C_RADER)  // the staged rows (stride a0.ncols) and X_0 per sequence after the tile
+    g.smem = (g.smem + 15) / 16 * 16 + (size_t)g.tpb * (a0.ncols + 1) * cplx_bytes(dtype);
   if (g.smem > kMaxSmem) return false;
   if (wide) {
     int th = threads_needed(sl, ept_of(dtype), g.tpb, false);

@@ -53,6 +53,87 @@ __global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_c2c(cons
   CoreT::run(a.core, a.tpb, sm, ld, st);
 }
 
+// ---------------------------------------------------------------- rows, Rader
+// A prime length N whose N - 1 = L is 7-smooth (N = 1009: L = 2^4 3^2 7)
+// by Rader's algorithm instead of Chirp-Z (src/chirpz.rs:87-146 computes
+// the same DFT with two FFTs of M = 2048). With g a primitive root mod N,
+//   X_0 = x_0 + sum_p a_p,   X_{g^-q} = x_0 + (a (*) b)_q,
+//   a_p = x_{g^p},  b_m = w_N^(g^-m),  (*) the cyclic convolution of length L,
+// so the core runs two L-point FFTs: FFT_L(a), times B^ = FFT_L(b) / L
+// (conjugated: the inverse runs as a forward FFT), FFT_L again. The rows are
+// staged contiguously in shared memory (buffer R, stride ldr); the first
+// FFT's first pass gathers a_p = R[g^p], its last pass stores the spectrum
+// product and keeps X_0 = x_0 + A_0; the second FFT's last pass scatters
+// x_0 + C_q to R[g^-q]; a contiguous store phase writes the rows out.
+// KArgs: aux0 = the permutations (L ints g^p mod N, then L ints g^-q mod N),
+// aux1 = B^ (L values), n_user = N, ncols = ldr; core = the L-point core.
+template <typename C>
+struct RaderGather {
+  const C* r;
+  int ldr;
+  const int* perm;  // g^p mod N
+  __device__ __forceinline__ C load(int t, int p) const { return r[t * ldr + __ldg(&perm[p])]; }
+};
+
+template <typename C, class Tile>
+struct RaderSpectrum {
+  const Tile& sm;
+  const C* bhat;  // FFT_L(b) / L
+  const C* r;
+  int ldr;
+  C* x0;          // per sequence: X_0 = x_0 + A_0
+  __device__ __forceinline__ void store(int t, int k, C v) const {
+    if (k == 0) x0[t] = cadd(r[t * ldr], v);
+    sm.store(t, k, cconj(cmul(v, __ldg(&bhat[k]))));
+  }
+};
+
+template <typename C>
+struct RaderScatter {
+  C* r;
+  int ldr;
+  const int* perm;  // g^-q mod N (never 0, so x_0 = R[0] stays readable)
+  __device__ __forceinline__ void store(int t, int q, C v) const {
+    r[t * ldr + __ldg(&perm[q])] = cadd(r[t * ldr], cconj(v));
+  }
+};
+
+template <typename T, class CoreT>
+__global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_c2c_rader(const KArgs a) {
+  using C = cx_t<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
+  const int L = a.core.n, N = a.n_user, ldr = a.ncols;
+  C* r = reinterpret_cast<C*>(smem_raw + (((size_t)a.tpb * a.ld * sizeof(C) + 15) / 16) * 16);
+  C* x0 = r + (size_t)a.tpb * ldr;
+  const long long t0 = (long long)blockIdx.x * a.tpb;
+  const int nvalid = (int)min((long long)a.tpb, a.count - t0);
+  const C* in = (const C*)a.in + t0 * a.in_dist;
+  for (int b = threadIdx.x; b < a.tpb * N; b += blockDim.x) {
+    const int t = b / N, i = b - t * N;
+    C v = czero<C>();
+    if (t < nvalid) {
+      v = cscale(in[(long long)t * a.in_dist + i], (T)a.scale);
+      if (a.back) v = cconj(v);
+    }
+    r[t * ldr + i] = v;
+  }
+  __syncthreads();
+  const int* perm = static_cast<const int*>(a.aux0);
+  RaderGather<C> gather{r, ldr, perm};
+  RaderSpectrum<C, decltype(sm)> spec{sm, static_cast<const C*>(a.aux1), r, ldr, x0};
+  CoreT::run(a.core, a.tpb, sm, gather, spec);
+  RaderScatter<C> scatter{r, ldr, perm + L};
+  CoreT::run(a.core, a.tpb, sm, sm, scatter);
+  __syncthreads();
+  C* out = (C*)a.out + t0 * a.out_dist;
+  for (int b = threadIdx.x; b < nvalid * N; b += blockDim.x) {
+    const int t = b / N, i = b - t * N;
+    const C v = i == 0 ? x0[t] : r[t * ldr + i];
+    out[(long long)t * a.out_dist + i] = a.back ? cconj(v) : v;
+  }
+}
+
 // ---------------------------------------------------------------- columns
 // Transform `count` arrays of core.n rows x ncols columns along the rows
 // dimension (each column is one sequence with stride ncols). A CTA takes
@@ -363,6 +444,9 @@ cudaError_t launch_complex(Kernel which, bool blue, bool k1, const KArgs& a, uns
         : (k1 ? K<T, DynCore<false, TMINOR, true, true>> : K<T, DynCore<false, TMINOR, true, false>>))
   switch (which) {
     case Kernel::C2C: fn = CHFFT_PICK(k_c2c, false); break;
+    case Kernel::C2C_RADER:
+      fn = k1 ? k_c2c_rader<T, DynCore<false, false, true, true>> : k_c2c_rader<T, DynCore<false, false, true, false>>;
+      break;
     case Kernel::COLS: fn = CHFFT_PICK(k_cols, true); break;
     default: return cudaErrorInvalidValue;
   }

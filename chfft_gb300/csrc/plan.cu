@@ -365,6 +365,93 @@ Geo row_geo(const Core& c, long long count, const PlanOpts& o) {
   return g;
 }
 
+Geo rader_geo(const RaderCore& r, long long count, const PlanOpts& o, int* ldr) {
+  Geo g = row_geo(r.lc, count, o);
+  *ldr = (int)(r.n | 1);
+  const size_t cb = cplx_bytes(r.dtype);
+  auto smem_for = [&](int tpb) {
+    return ((size_t)tpb * g.ld * cb + 15) / 16 * 16 + (size_t)tpb * (*ldr + 1) * cb;
+  };
+  // Keep two CTAs' tiles within an SM's shared memory, as row_geo does.
+  while (g.tpb > 1 && smem_for(g.tpb) > kMaxSmem / 2) g.tpb--;
+  g.threads = std::min(kMaxThreads, std::max(32, (threads_needed(r.lc.st, ept_of(r.dtype), g.tpb, g.k1) + 31) / 32 * 32));
+  g.smem = smem_for(g.tpb);
+  return g;
+}
+
+namespace {
+long long mulmod(long long a, long long b, long long m) { return (long long)((__int128)a * b % m); }
+long long powmod(long long a, long long e, long long m) {
+  long long r = 1 % m;
+  a %= m;
+  for (; e > 0; e >>= 1, a = mulmod(a, a, m))
+    if (e & 1) r = mulmod(r, a, m);
+  return r;
+}
+bool is_prime(long long n) {
+  if (n < 2) return false;
+  for (long long d = 2; d * d <= n; d++)
+    if (n % d == 0) return false;
+  return true;
+}
+}  // namespace
+
+bool RaderCore::build(long long n_, int dtype_, cudaStream_t s) {
+  release();
+  const long long L_ = n_ - 1;
+  if (n_ < 11 || n_ > (1LL << 24) || !is_prime(n_)) return false;
+  StageList st;
+  if (!make_stages(L_, &st) || !fits_cta(st, dtype_)) return false;
+  // One sequence's tile, staged row and X_0 slot must fit a CTA (with room
+  // for the plan-time kernels' wider tile stride).
+  const size_t cb = cplx_bytes(dtype_);
+  if ((size_t)(smem_ld(L_) + 64) * cb + (size_t)((n_ | 1) + 1) * cb + 16 > kMaxSmem) return false;
+  // The least primitive root: g^(L/q) != 1 for every prime q | L (q in 2, 3, 5, 7).
+  int root = 0;
+  for (int cand = 2; cand < n_ && !root; cand++) {
+    bool ok = true;
+    for (int q : {2, 3, 5, 7})
+      if (L_ % q == 0 && powmod(cand, L_ / q, n_) == 1) ok = false;
+    if (ok) root = cand;
+  }
+  if (!root || !lc.build(L_, dtype_, s)) return false;
+  n = n_;
+  L = (int)L_;
+  g = root;
+  dtype = dtype_;
+  std::vector<int> pm(2 * (size_t)L);
+  std::vector<double2> b(L);
+  const long long ginv = powmod(root, L_ - 1, n_);
+  long long gp = 1, gq = 1;
+  for (int i = 0; i < L; i++) {
+    pm[i] = (int)gp;        // g^i
+    pm[L + i] = (int)gq;    // g^-i
+    // b_i = w_n^(g^-i) / L, FP64 with the numerator reduced to (-n/2, n/2]
+    long long e = gq;
+    if (2 * e > n_) e -= n_;
+    const double ang = -2.0 * M_PI * (double)e / (double)n_;
+    b[i] = make_double2(std::cos(ang) / (double)L, std::sin(ang) / (double)L);
+    gp = mulmod(gp, root, n_);
+    gq = mulmod(gq, ginv, n_);
+  }
+  perm.ensure(pm.size() * sizeof(int));
+  CHFFT_CUDA(cudaMemcpyAsync(perm.p, pm.data(), pm.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+  // B^ = FFT_L(b) by the FP64 core, rounded once to the working dtype.
+  DevBuf b64;
+  b64.ensure((size_t)L * sizeof(double2));
+  CHFFT_CUDA(cudaMemcpyAsync(b64.p, b.data(), (size_t)L * sizeof(double2), cudaMemcpyHostToDevice, s));
+  Core c64;
+  if (!c64.build(L_, 1, s)) return false;
+  fft_f64_inplace(static_cast<double2*>(b64.p), c64, s);
+  bhat.ensure((size_t)L * cplx_bytes(dtype));
+  if (dtype == 0)
+    CHFFT_CUDA(convert_from_f64<float>(static_cast<const double2*>(b64.p), bhat.p, L, s));
+  else
+    CHFFT_CUDA(cudaMemcpyAsync(bhat.p, b64.p, (size_t)L * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+  CHFFT_CUDA(cudaStreamSynchronize(s));  // the host tables and b64 are freed on return
+  return true;
+}
+
 Geo col_geo(const Core& c, int ncols, int tpb_opt, const PlanOpts& o) {
   Geo g;
   g.max_radix = o.max_radix == 16 ? 16 : 32;

@@ -125,6 +125,24 @@ struct Core {
   size_t device_bytes() const { return tw.bytes + chirp.bytes + bhat.bytes + stw.bytes + wide.bytes + tcw.bytes; }
 };
 
+// Rader's algorithm for a prime n whose n - 1 = L is 7-smooth and fits one
+// CTA (k_c2c_rader): the L-point core, the permutations g^p and g^-q mod n
+// (g the least primitive root), and B^ = FFT_L(b) / L, b_m = w_n^(g^-m),
+// computed in FP64 and rounded once.
+struct RaderCore {
+  long long n = 0;
+  int L = 0, g = 0, dtype = 0;
+  Core lc;
+  DevBuf perm, bhat;
+  bool build(long long n, int dtype, cudaStream_t s);  // false: n does not qualify
+  void release() {
+    n = 0;
+    perm.release();
+    bhat.release();
+  }
+  size_t device_bytes() const { return lc.device_bytes() + perm.bytes + bhat.bytes; }
+};
+
 // Launch geometry of a CTA-per-`tpb`-sequences kernel.
 struct Geo {
   int tpb = 1, threads = 32;
@@ -138,6 +156,9 @@ struct Geo {
 };
 Geo row_geo(const Core& c, long long count, const PlanOpts& o = PlanOpts{});
 Geo col_geo(const Core& c, int ncols, int tpb_opt = 0, const PlanOpts& o = PlanOpts{});
+// Rader rows: the L-point core's geometry with the staged rows (stride
+// *ldr) and X_0 slots added to the shared memory.
+Geo rader_geo(const RaderCore& r, long long count, const PlanOpts& o, int* ldr);
 
 // Smallest 7-smooth M >= lo that the CTA engine runs cheapest (M * passes).
 long long bluestein_length(long long n, int dtype);

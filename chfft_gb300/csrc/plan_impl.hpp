@@ -92,6 +92,11 @@ struct PlanImpl {
   Core core2;  // CFft2D columns: M
   BigCore big;           // CFft1D beyond one CTA (four-step)
   bool use_big = false;
+  // CFft1D of a prime length with a 7-smooth n - 1: Rader's algorithm
+  // instead of Chirp-Z (CHFFT_RADER=0 or an explicit Bluestein length keep
+  // Chirp-Z); `core` still holds the Chirp-Z core for the other paths.
+  RaderCore rader;
+  bool use_rader = false;
   PlanOpts opts;         // tuning knobs (chfft_plan_set_config)
   DevBuf work;           // four-step workspace
   DevBuf aux0, aux1;
@@ -132,13 +137,19 @@ struct PlanImpl {
     };
     use_big = false;
     switch (kind) {
-      case CHFFT_KIND_CFFT1D:
+      case CHFFT_KIND_CFFT1D: {
         if (len >= 2 && !core.build(len, dtype, s, opts.blue_m)) {
           if (!big.build(len, dtype, s, opts))
             throw Fail{CHFFT_EUNSUPPORTED, "transform length " + std::to_string(len) + " is not supported"};
           use_big = true;
         }
+        use_rader = false;
+        rader.release();
+        const char* e = std::getenv("CHFFT_RADER");
+        const bool rader_ok = !(e && e[0] == '0') && opts.blue_m == 0;
+        if (!use_big && core.blue && rader_ok) use_rader = rader.build(len, dtype, s);
         break;
+      }
       case CHFFT_KIND_CFFT2D:
         if (len_m > 0 && len_n > 0) {
           need(core, len_n);
@@ -183,7 +194,7 @@ struct PlanImpl {
   // Applies tuning knobs; the tables are rebuilt when the Bluestein length
   // or the four-step split changes.
   void apply(const PlanOpts& o) {
-    const bool rebuild = o.blue_m != opts.blue_m || o.fs_n1 != opts.fs_n1;
+    const bool rebuild = o.blue_m != opts.blue_m || o.fs_n1 != opts.fs_n1;  // (also decides Rader vs Chirp-Z)
     opts = o;
     big.opts = o;
     if (rebuild) build();
@@ -273,6 +284,22 @@ struct PlanImpl {
   }
 
   template <typename T>
+  void launch_rader(KArgs& a, long long count, cudaStream_t s) {
+    int ldr = 0;
+    Geo g = rader_geo(rader, count, opts, &ldr);
+    a.core = rader.lc.desc();
+    a.tpb = g.tpb;
+    a.ld = g.ld;
+    a.count = count;
+    a.aux0 = rader.perm.p;
+    a.aux1 = rader.bhat.p;
+    a.n_user = (int)rader.n;
+    a.ncols = ldr;
+    const unsigned blocks = (unsigned)((count + g.tpb - 1) / g.tpb);
+    dispatch<T>(Kernel::C2C_RADER, rader.lc, g, a, blocks, count * rader.n, s);
+  }
+
+  template <typename T>
   void exec_t(const MethodSpec& ms, const void* d_in, void* d_out, long long batch, cudaStream_t s) {
     const double sc = scale_value(ms.scale);
     KArgs a{};
@@ -293,6 +320,10 @@ struct PlanImpl {
           return;
         }
         a.in_dist = a.out_dist = len;
+        if (use_rader && opts.tc <= 0) {
+          launch_rader<T>(a, batch, s);
+          return;
+        }
         launch<T>(Kernel::C2C, core, a, batch, s);
         return;
       case CHFFT_KIND_CFFT2D: {

@@ -325,3 +325,39 @@ def test_config_4096x16384_fp32_outliers_every_row():
         ref = np.fft.fft(x[lo:lo + 2048].astype(np.complex128), axis=-1)
         err = np.linalg.norm(y[lo:lo + 2048] - ref, axis=-1) / np.linalg.norm(ref, axis=-1)
         assert err.max() <= 1e-6, (lo, float(err.max()))
+
+
+# ---------------------------------------------------------------- Rader
+@pytest.mark.parametrize("dt", DTYPES)
+@pytest.mark.parametrize("n", [17, 31, 1009, 7681, 12289])
+def test_rader_lengths(n, dt):
+    """Primes whose n - 1 is 7-smooth run Rader's algorithm (two (n-1)-point
+    FFTs) instead of Chirp-Z; same results as the oracle's Chirp-Z
+    (src/chirpz.rs) within the tolerances, every method, and the same as the
+    Chirp-Z path of this library (CHFFT_RADER=0)."""
+    import os
+
+    p = cg.CFft1D.with_len(n, dt)
+    info = p.info()
+    if dt == np.float64 and n == 12289:
+        assert info.algorithm == 1  # the staged row does not fit a CTA in f64: Chirp-Z
+    else:
+        assert info.algorithm == 4
+    x = rng_vectors(n, count=3).astype(CPLX[dt])
+    xd = x.astype(np.complex128)
+    for fwd, bwd in SCALED:
+        y = p.execute_batch(fwd, x)
+        for i in range(3):
+            close(y[i], oracle.cfft1d(xd[i], fwd), dt)
+        z = p.execute_batch(bwd, y)
+        close(z, xd, dt)
+    y = x.copy()
+    p.forward0i(y[0])
+    close(y[0], oracle.cfft1d(xd[0], "forward0"), dt)
+    os.environ["CHFFT_RADER"] = "0"
+    try:
+        q = cg.CFft1D.with_len(n, dt)
+        assert q.info().algorithm == 1
+        close(q.execute_batch("forward", x), p.execute_batch("forward", x).astype(np.complex128), dt)
+    finally:
+        os.environ.pop("CHFFT_RADER", None)

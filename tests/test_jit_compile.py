@@ -4,8 +4,8 @@ The library compiles these at plan time on the GPU host (csrc/jit.cu), and a
 failed compile there falls back to the run-time-stage library kernels, so a
 header change that breaks them would only show as slower plans. This test
 hands NVRTC the same headers, options and name expressions (the instances
-of the benchmark's plans, the four-step passes and the Bluestein middle
-pass) and checks that each compiles, and that the
+of the benchmark's plans, the four-step passes, the Bluestein middle pass
+and the Rader rows) and checks that each compiles, and that the
 hot ones stay free of register spills. NVRTC needs no GPU.
 """
 import ctypes
@@ -62,6 +62,8 @@ CASES = [
     (f"&chfft::kern::k_rows_t<float, {A_2P20}, 0>", True),
     (f"&chfft::kern::k_rows_t<float, {A_2P20}, 2>", False),
     ("&chfft::kern::k_rows_bb<float, chfft::StatCore<false,true,true,512,512,8,546,16,256,4,0,16,16,2>, 3>", True),
+    # Rader rows of N = 1009 (the 1008-point core, one sequence per CTA)
+    ("&chfft::kern::k_c2c_rader<float, chfft::StatCore<false,false,true,1008,1008,1,1071,16,352,2,0,16,3,3,7>>", True),
     ("&chfft::kern::k_rows_bb<double, chfft::StatCore<false,true,false,256,256,4,274,16,256,1,0,16,16>, 7>", False),
 ]
 

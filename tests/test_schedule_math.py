@@ -91,3 +91,40 @@ def test_pipe_ticket_order(count, ta, tb, lead, ring):
             assert all(pos[(False, k - ring, x)] < t for x in range(tb))
         if not is_a:  # waits for every A(k) tile
             assert all(pos[(True, k, x)] < t for x in range(ta))
+
+
+def rader(x):
+    """Rader's algorithm as k_c2c_rader computes it: a_p = x[g^p], B^ = FFT_L(b) / L
+    with b_m = w_N^(g^-m), the inverse as a conjugated forward FFT, x_0 + C_q
+    scattered to g^-q, X_0 = x_0 + A_0."""
+    n = x.size
+    L = n - 1
+    g = next(c for c in range(2, n) if all(L % q or pow(c, L // q, n) != 1 for q in (2, 3, 5, 7)))
+    ginv = pow(g, L - 1, n)
+    p_in = np.array([pow(g, i, n) for i in range(L)])
+    p_out = np.array([pow(ginv, i, n) for i in range(L)])
+    assert sorted(p_in) == list(range(1, n)) and sorted(p_out) == list(range(1, n)) and 0 not in p_out
+    b = np.exp(-2j * np.pi * p_out / n) / L
+    bhat = np.fft.fft(b)
+    A = np.fft.fft(x[p_in])
+    spec = np.conj(A * bhat)
+    C = np.conj(np.fft.fft(spec))
+    out = np.empty(n, complex)
+    out[p_out] = x[0] + C
+    out[0] = x[0] + A[0]
+    return out
+
+
+@pytest.mark.parametrize("n", [11, 13, 17, 29, 31, 97, 257, 1009, 7681, 12289])
+def test_rader_matches_dft(n):
+    L = n - 1
+    while L % 2 == 0:
+        L //= 2
+    for q in (3, 5, 7):
+        while L % q == 0:
+            L //= q
+    assert L == 1  # n - 1 is 7-smooth
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    ref = np.fft.fft(x)
+    assert np.linalg.norm(rader(x) - ref) / np.linalg.norm(ref) < 1e-12
