@@ -339,8 +339,8 @@ def test_rader_lengths(n, dt):
 
     p = cg.CFft1D.with_len(n, dt)
     info = p.info()
-    if dt == np.float64 and n == 12289:
-        assert info.algorithm == 1  # the staged row does not fit a CTA in f64: Chirp-Z
+    if dt == np.float64 and n >= 7681:
+        assert info.algorithm in (1, 3)  # tile and staged row do not fit a CTA in f64: Chirp-Z
     else:
         assert info.algorithm == 4
     x = rng_vectors(n, count=3).astype(CPLX[dt])
@@ -357,7 +357,7 @@ def test_rader_lengths(n, dt):
     os.environ["CHFFT_RADER"] = "0"
     try:
         q = cg.CFft1D.with_len(n, dt)
-        assert q.info().algorithm == 1
+        assert q.info().algorithm in (1, 3)
         close(q.execute_batch("forward", x), p.execute_batch("forward", x).astype(np.complex128), dt)
     finally:
         os.environ.pop("CHFFT_RADER", None)
