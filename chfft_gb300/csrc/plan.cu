@@ -440,9 +440,19 @@ bool RaderCore::build(long long n_, int dtype_, cudaStream_t s) {
   DevBuf b64;
   b64.ensure((size_t)L * sizeof(double2));
   CHFFT_CUDA(cudaMemcpyAsync(b64.p, b.data(), (size_t)L * sizeof(double2), cudaMemcpyHostToDevice, s));
-  Core c64;
-  if (!c64.build(L_, 1, s)) return false;
-  fft_f64_inplace(static_cast<double2*>(b64.p), c64, s);
+  StageList st64;
+  if (make_stages(L_, &st64) && fits_cta(st64, 1)) {
+    Core c64;
+    if (!c64.build(L_, 1, s)) return false;
+    fft_f64_inplace(static_cast<double2*>(b64.p), c64, s);
+  } else {  // the FP64 four-step engine
+    BigCore big64;
+    DevBuf w64;
+    if (!big64.build(L_, 1, s)) return false;
+    w64.ensure(big64.work_elems(1) * sizeof(double2));
+    big64.exec(b64.p, b64.p, w64.p, 1, false, 1.0, s);
+    CHFFT_CUDA(cudaStreamSynchronize(s));
+  }
   bhat.ensure((size_t)L * cplx_bytes(dtype));
   if (dtype == 0)
     CHFFT_CUDA(convert_from_f64<float>(static_cast<const double2*>(b64.p), bhat.p, L, s));
