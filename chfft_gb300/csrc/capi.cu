@@ -256,23 +256,26 @@ int chfft_plan_get_info(chfft_plan plan, chfft_plan_info* info) {
   info->len = (size_t)p.len;
   info->len_m = (size_t)p.len_m;
   info->len_n = (size_t)p.len_n;
-  info->fft_len = (size_t)(p.use_big ? p.big.n : p.core.n);
+  info->fft_len = (size_t)(p.use_big ? p.big.n : p.use_rader ? p.rader.n : p.core.n);
   info->algorithm = p.use_big ? (p.big.blue ? 3 : 2) : p.use_rader ? 4 : (p.core.blue ? 1 : 0);
   info->padded_len = p.use_big ? (p.big.blue ? (size_t)p.big.m : 0)
                                : p.use_rader ? 0 : (p.core.blue ? (size_t)p.core.st.n : 0);
+  // Rader plans report their (n - 1)-point core's passes and geometry.
+  const chfft::Core& cc = p.use_rader ? p.rader.lc : p.core;
   int k = 0;
-  if (p.core.st.npass >= 2) {
-    info->radix[k++] = p.core.st.rf;
+  if (cc.st.npass >= 2) {
+    info->radix[k++] = cc.st.rf;
     for (int i = 0; i < chfft::kNumRadix; i++)
-      for (int c = 0; c < p.core.st.mid[i] && k < 24; c++) info->radix[k++] = chfft::radix_at(i);
-    if (k < 24) info->radix[k++] = p.core.st.rl;
+      for (int c = 0; c < cc.st.mid[i] && k < 24; c++) info->radix[k++] = chfft::radix_at(i);
+    if (k < 24) info->radix[k++] = cc.st.rl;
   } else {
     for (int i = 0; i < chfft::kNumRadix; i++)
-      for (int c = 0; c < p.core.st.all[i] && k < 24; c++) info->radix[k++] = chfft::radix_at(i);
+      for (int c = 0; c < cc.st.all[i] && k < 24; c++) info->radix[k++] = chfft::radix_at(i);
   }
   info->npass = k;
-  if (p.core.n > 0) {
-    chfft::Geo g = chfft::row_geo(p.core, 1 << 20);
+  if (cc.n > 0) {
+    int ldr = 0;
+    chfft::Geo g = p.use_rader ? chfft::rader_geo(p.rader, 1 << 20, p.opts, &ldr) : chfft::row_geo(p.core, 1 << 20);
     info->seq_per_cta = g.tpb;
     info->threads_per_cta = g.threads;
     info->smem_per_cta = g.smem;

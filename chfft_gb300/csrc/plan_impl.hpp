@@ -138,16 +138,19 @@ struct PlanImpl {
     use_big = false;
     switch (kind) {
       case CHFFT_KIND_CFFT1D: {
-        if (len >= 2 && !core.build(len, dtype, s, opts.blue_m)) {
+        use_rader = false;
+        rader.release();
+        const bool one_cta = len < 2 || core.build(len, dtype, s, opts.blue_m);
+        if (len >= 2 && (!one_cta || core.blue)) {
+          // A prime length: Rader when its n - 1 core fits one CTA.
+          const char* e = std::getenv("CHFFT_RADER");
+          if (!(e && e[0] == '0') && opts.blue_m == 0) use_rader = rader.build(len, dtype, s);
+        }
+        if (!one_cta && !use_rader) {
           if (!big.build(len, dtype, s, opts))
             throw Fail{CHFFT_EUNSUPPORTED, "transform length " + std::to_string(len) + " is not supported"};
           use_big = true;
         }
-        use_rader = false;
-        rader.release();
-        const char* e = std::getenv("CHFFT_RADER");
-        const bool rader_ok = !(e && e[0] == '0') && opts.blue_m == 0;
-        if (!use_big && core.blue && rader_ok) use_rader = rader.build(len, dtype, s);
         break;
       }
       case CHFFT_KIND_CFFT2D:
