@@ -130,10 +130,7 @@ const char* kernel_template(Kernel k) {
 
 // Tile pad period of a specialised kernel: the first pass's radix when even
 // (its stride-R stores then become conflict-free), no padding otherwise.
-int pad_period(const StageList& st) {
-  std::vector<int> order = pass_order(st);
-  return (!order.empty() && order[0] % 2 == 0) ? order[0] : 0;
-}
+int pad_period(const std::vector<int>& order) { return (!order.empty() && order[0] % 2 == 0) ? order[0] : 0; }
 
 bool column_mapped(Kernel k) {
   return k == Kernel::COLS || k == Kernel::COLS_TW || k == Kernel::ROWS_T || k == Kernel::ROWS_BB;
@@ -144,9 +141,9 @@ bool four_step(Kernel k) { return k == Kernel::COLS_TW || k == Kernel::ROWS_T ||
 // of one shared-memory wavefront (16 f32 / 8 f64 complex elements) tpb
 // adjacent sequences times q = lanes / tpb adjacent elements; a stride that
 // is q times an odd number puts all of them in distinct banks.
-int tile_ld(const StageList& st, int tpb, int dtype, bool column) {
-  const int p = pad_period(st);
-  int ld = st.n + (p > 0 ? st.n / p : 0);
+int tile_ld(int n, const std::vector<int>& order, int tpb, int dtype, bool column) {
+  const int p = pad_period(order);
+  int ld = n + (p > 0 ? n / p : 0);
   const int lanes = dtype == 0 ? 16 : 8;
   const int q = column ? std::max(1, lanes / std::max(1, tpb)) : 1;
   while (ld % (2 * q) != q) ld++;
@@ -154,7 +151,7 @@ int tile_ld(const StageList& st, int tpb, int dtype, bool column) {
 }
 
 // "chfft::StatCore<...>" of a specialised kernel.
-std::string core_expression(Kernel k, int dtype, const Core& c, const StageList& sl, const Geo& g) {
+std::string core_expression(Kernel k, int dtype, const Core& c, int n, const std::vector<int>& order, const Geo& g) {
   std::string s = "chfft::StatCore<";
   s += c.blue ? "true," : "false,";
   s += column_mapped(k) ? "true," : "false,";
@@ -164,23 +161,26 @@ std::string core_expression(Kernel k, int dtype, const Core& c, const StageList&
   // one-butterfly complex kernels of radices up to 10, which fit it without
   // spilling (N = 1000: 30 -> 27 us measured).
   int rmax = 0;
-  for (int r : pass_order(sl)) rmax = std::max(rmax, r);
+  for (int r : order) rmax = std::max(rmax, r);
   const bool small_radix = dtype == 0 && rmax <= 10 && !c.blue && (k == Kernel::C2C || k == Kernel::COLS);
-  const int per512 = g.k1 ? (small_radix ? 3 : 2) : (g.ept > 0 ? 2 : 1);
+  // Rader rows hold up to 64 elements per thread in their two passes and fit
+  // two CTAs per SM by shared memory: the register budget of two 512-thread CTAs.
+  const int per512 = k == Kernel::C2C_RADER ? 1 : g.k1 ? (small_radix ? 3 : 2) : (g.ept > 0 ? 2 : 1);
   const int minb = g.min_blocks > 0 ? g.min_blocks : std::max(1, per512 * (kMaxThreads / std::max(32, g.threads)));
-  s += std::to_string(sl.n) + "," + std::to_string(c.n) + "," + std::to_string(g.tpb) + "," + std::to_string(g.ld) +
-       "," + std::to_string(pad_period(sl)) + "," + std::to_string(g.threads) + "," + std::to_string(minb) + "," +
+  s += std::to_string(n) + "," + std::to_string(c.n) + "," + std::to_string(g.tpb) + "," + std::to_string(g.ld) +
+       "," + std::to_string(pad_period(order)) + "," + std::to_string(g.threads) + "," + std::to_string(minb) + "," +
        std::to_string(g.k1 ? 0 : g.ept);
-  for (int r : pass_order(sl)) s += "," + std::to_string(r);
+  for (int r : order) s += "," + std::to_string(r);
   s += ">";
   return s;
 }
 
-std::string name_expression(Kernel k, int dtype, const Core& c, const StageList& sl, const Geo& g, int mode) {
+std::string name_expression(Kernel k, int dtype, const Core& c, int n, const std::vector<int>& order, const Geo& g,
+                            int mode) {
   std::string s = "&";
   s += kernel_template(k);
   s += dtype == 0 ? "<float, " : "<double, ";
-  s += core_expression(k, dtype, c, sl, g);
+  s += core_expression(k, dtype, c, n, order, g);
   if (four_step(k)) s += ", " + std::to_string(mode);
   s += ">";
   return s;
@@ -252,6 +252,7 @@ namespace {
 struct Spec {
   Geo g;
   const StageList* sl = nullptr;
+  std::vector<int> order;  // the passes' radices, first pass first
   KArgs a;
 };
 
@@ -259,6 +260,27 @@ struct Spec {
 bool resolve(Kernel k, int dtype, const Core& c, const Geo& g0, const KArgs& a0, int mode, const FourStep* fs,
              Spec* out) {
   if (!c.stw.p) return false;
+  if (k == Kernel::C2C_RADER && !c.order2.empty() && c.stw2.p) {
+    // The Rader core's two-pass order, one butterfly per thread, on the
+    // host's sequences per CTA.
+    Geo g = g0;
+    int per_seq = 0;
+    for (int r : c.order2) per_seq = std::max(per_seq, (int)(c.st.n / r));
+    g.k1 = true;
+    g.ept = 0;
+    g.threads = std::max(32, (g.tpb * per_seq + 31) / 32 * 32);
+    if (g.threads > kMaxThreads) return false;
+    g.ld = tile_ld(c.st.n, c.order2, g.tpb, dtype, false);
+    g.smem = ((size_t)g.tpb * g.ld * cplx_bytes(dtype) + 15) / 16 * 16 + (size_t)g.tpb * (a0.ncols + 1) * cplx_bytes(dtype);
+    if (g.smem > kMaxSmem) return false;
+    out->a = a0;
+    out->a.ld = g.ld;
+    out->a.core.stw = c.stw2.p;
+    out->g = g;
+    out->sl = &c.st;
+    out->order = c.order2;
+    return true;
+  }
   // Stage list: the radix-32 one where every thread holds 32 elements.
   const bool wide = !g0.k1 && g0.ept == 0 && g0.max_radix >= 32 && c.wide.p;
   const StageList& sl = wide ? c.sw : c.st;
@@ -282,7 +304,7 @@ bool resolve(Kernel k, int dtype, const Core& c, const Geo& g0, const KArgs& a0,
       g.threads = std::max(32, ((th + 31) / 32) * 32);
     }
   }
-  g.ld = tile_ld(sl, g.tpb, dtype, column_mapped(k));
+  g.ld = tile_ld(sl.n, pass_order(sl), g.tpb, dtype, column_mapped(k));
   g.smem = (size_t)g.tpb * g.ld * cplx_bytes(dtype);
   if (k == Kernel::COLS_TW && (mode & 8) && fs)  // pass A's twiddle tables after the tile
     g.smem = (g.smem + 15) / 16 * 16 + (size_t)smem_twiddle_entries(g.tpb, fs->n1) * cplx_bytes(dtype);
@@ -303,6 +325,7 @@ bool resolve(Kernel k, int dtype, const Core& c, const Geo& g0, const KArgs& a0,
   }
   out->g = g;
   out->sl = &sl;
+  out->order = pass_order(sl);
   return true;
 }
 
@@ -341,7 +364,7 @@ int jit_launch(Kernel k, int dtype, const Core& c, const Geo& g0, const KArgs& a
   const Geo& g = sp.g;
   KArgs& a = sp.a;
   CUfunction fn = nullptr;
-  const std::string expr = name_expression(k, dtype, c, *sp.sl, g, mode);
+  const std::string expr = name_expression(k, dtype, c, sp.sl->n, sp.order, g, mode);
   if (int r = kernel_for(expr, g.smem, &fn)) return r;
   void* args[] = {const_cast<KArgs*>(&a), const_cast<FourStep*>(fs)};
   if (g_api.cuLaunchKernel(fn, blocks, 1, 1, g.threads, 1, 1, (unsigned)g.smem, (CUstream)stream, args, nullptr) != 0)

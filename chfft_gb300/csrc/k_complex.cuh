@@ -109,14 +109,25 @@ __global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_c2c_rade
   const long long t0 = (long long)blockIdx.x * a.tpb;
   const int nvalid = (int)min((long long)a.tpb, a.count - t0);
   const C* in = (const C*)a.in + t0 * a.in_dist;
-  for (int b = threadIdx.x; b < a.tpb * N; b += blockDim.x) {
-    const int t = b / N, i = b - t * N;
-    C v = czero<C>();
-    if (t < nvalid) {
-      v = cscale(in[(long long)t * a.in_dist + i], (T)a.scale);
-      if (a.back) v = cconj(v);
+  // Stage the rows, kU loads in flight per thread before their stores.
+  constexpr int kU = 8;
+  const int total = a.tpb * N;
+  for (int b0 = threadIdx.x; b0 < total; b0 += kU * blockDim.x) {
+    C v[kU];
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const int b = b0 + u * blockDim.x, t = b / N, i = b - t * N;
+      v[u] = czero<C>();
+      if (b < total && t < nvalid) v[u] = in[(long long)t * a.in_dist + i];
     }
-    r[t * ldr + i] = v;
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const int b = b0 + u * blockDim.x, t = b / N, i = b - t * N;
+      if (b < total) {
+        const C w = cscale(v[u], (T)a.scale);
+        r[t * ldr + i] = a.back ? cconj(w) : w;
+      }
+    }
   }
   __syncthreads();
   const int* perm = static_cast<const int*>(a.aux0);

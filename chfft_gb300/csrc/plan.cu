@@ -237,6 +237,8 @@ bool Core::build(long long n_, int dtype_, cudaStream_t s, long long blue_m) {
   stw.release();
   wide.release();
   tcw.release();
+  order2.clear();
+  stw2.release();
   tc_r0 = tc_s16 = 0;
   const size_t cb = cplx_bytes(dtype);
   if (n == 1) {
@@ -366,7 +368,12 @@ Geo row_geo(const Core& c, long long count, const PlanOpts& o) {
 }
 
 Geo rader_geo(const RaderCore& r, long long count, const PlanOpts& o, int* ldr) {
-  Geo g = row_geo(r.lc, count, o);
+  // Several butterflies per thread unless the k1 knob asks otherwise: the
+  // (n - 1)-point cores mix radices 16, 7 and 3 (1008 = 16 3 3 7), whose
+  // one-butterfly geometry leaves most threads idle in the radix-16 pass.
+  PlanOpts q = o;
+  if (q.k1 < 0) q.k1 = 0;
+  Geo g = row_geo(r.lc, count, q);
   *ldr = (int)(r.n | 1);
   const size_t cb = cplx_bytes(r.dtype);
   auto smem_for = [&](int tpb) {
@@ -415,6 +422,27 @@ bool RaderCore::build(long long n_, int dtype_, cudaStream_t s) {
     if (ok) root = cand;
   }
   if (!root || !lc.build(L_, dtype_, s)) return false;
+  // Two passes for the plan-time f32 kernels: L = r1 r2 with both radices at
+  // most 64, as close to sqrt(L) as possible (1008 = 28 x 36). (f64 keeps the
+  // standard order: 64 complex doubles per thread spill.)
+  lc.order2.clear();
+  lc.stw2.release();
+  for (long long d = 2, best = 1LL << 40; dtype_ == 0 && d <= 64; d++) {
+    if (L_ % d || L_ / d > 64 || !factor_smooth(d).ok || !factor_smooth(L_ / d).ok) continue;
+    const long long spread = std::llabs(L_ / d - d);
+    if (spread < best || (spread == best && d < L_ / d)) {
+      best = spread;
+      lc.order2 = {(int)d, (int)(L_ / d)};
+    }
+  }
+  if (!lc.order2.empty()) {
+    PassList pl{};
+    pl.npass = 2;
+    pl.r[0] = lc.order2[0];
+    pl.r[1] = lc.order2[1];
+    lc.stw2.ensure((size_t)(L_ - 1) * cplx_bytes(dtype_));
+    CHFFT_CUDA(dtype_ == 0 ? gen_stage_table<float>(pl, lc.stw2.p, s) : gen_stage_table<double>(pl, lc.stw2.p, s));
+  }
   n = n_;
   L = (int)L_;
   g = root;

@@ -116,13 +116,18 @@ struct Core {
   // Tensor-core pass order (r0, 16, ..., 16), n = r0 * 16^tc_s16 (f32, power
   // of two), and its stage twiddles; tc_s16 = 0 when n does not qualify.
   int tc_r0 = 0, tc_s16 = 0;
-  DevBuf tw, chirp, bhat, stw, wide, tcw;
+  // Rader cores: a two-pass order (two radices of at most 64) for the
+  // plan-time Rader kernels, and its stage twiddles; empty otherwise.
+  std::vector<int> order2;
+  DevBuf tw, chirp, bhat, stw, wide, tcw, stw2;
   bool build(long long n, int dtype, cudaStream_t s, long long blue_m = 0);  // false: unsupported size
   void build_wide(cudaStream_t s);  // also the tensor-core pass order
   void build_tc(cudaStream_t s);
   CoreDesc desc() const;
   long long fft_len() const { return st.n; }
-  size_t device_bytes() const { return tw.bytes + chirp.bytes + bhat.bytes + stw.bytes + wide.bytes + tcw.bytes; }
+  size_t device_bytes() const {
+    return tw.bytes + chirp.bytes + bhat.bytes + stw.bytes + wide.bytes + tcw.bytes + stw2.bytes;
+  }
 };
 
 // Rader's algorithm for a prime n whose n - 1 = L is 7-smooth and fits one

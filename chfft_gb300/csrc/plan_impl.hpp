@@ -93,8 +93,10 @@ struct PlanImpl {
   BigCore big;           // CFft1D beyond one CTA (four-step)
   bool use_big = false;
   // CFft1D of a prime length with a 7-smooth n - 1: Rader's algorithm
-  // instead of Chirp-Z (CHFFT_RADER=0 or an explicit Bluestein length keep
-  // Chirp-Z); `core` still holds the Chirp-Z core for the other paths.
+  // instead of Chirp-Z when CHFFT_RADER=1 (measured slower than the fused
+  // Chirp-Z core on GB300: N = 1009 x 4096 66 us against 47 us; the staged
+  // row doubles the shared memory per sequence). `core` still holds the
+  // Chirp-Z core for the other paths.
   RaderCore rader;
   bool use_rader = false;
   PlanOpts opts;         // tuning knobs (chfft_plan_set_config)
@@ -144,7 +146,7 @@ struct PlanImpl {
         if (len >= 2 && (!one_cta || core.blue)) {
           // A prime length: Rader when its n - 1 core fits one CTA.
           const char* e = std::getenv("CHFFT_RADER");
-          if (!(e && e[0] == '0') && opts.blue_m == 0) use_rader = rader.build(len, dtype, s);
+          if (e && e[0] == '1' && opts.blue_m == 0) use_rader = rader.build(len, dtype, s);
         }
         if (!one_cta && !use_rader) {
           if (!big.build(len, dtype, s, opts))

@@ -222,7 +222,8 @@ typedef struct chfft_plan_info {
   size_t len, len_m, len_n;  /* user lengths */
   size_t fft_len;            /* length of the complex core FFT */
   int algorithm;             /* 0 mixed radix in shared memory, 1 fused Bluestein, 2 four-step, 3 four-step Bluestein,
-                                4 Rader (CFft1D of a prime length whose length - 1 is 7-smooth; rows fit one CTA) */
+                                4 Rader (CFft1D of a prime length whose length - 1 is 7-smooth, rows fitting one
+                                CTA, with CHFFT_RADER=1 at plan creation; Chirp-Z otherwise) */
   size_t padded_len;         /* Bluestein convolution length M (0 otherwise) */
   int npass;                 /* radix passes of the core FFT */
   int radix[24];

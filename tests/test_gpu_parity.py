@@ -331,13 +331,17 @@ def test_config_4096x16384_fp32_outliers_every_row():
 @pytest.mark.parametrize("dt", DTYPES)
 @pytest.mark.parametrize("n", [17, 31, 1009, 7681, 12289])
 def test_rader_lengths(n, dt):
-    """Primes whose n - 1 is 7-smooth run Rader's algorithm (two (n-1)-point
-    FFTs) instead of Chirp-Z; same results as the oracle's Chirp-Z
-    (src/chirpz.rs) within the tolerances, every method, and the same as the
-    Chirp-Z path of this library (CHFFT_RADER=0)."""
+    """With CHFFT_RADER=1, primes whose n - 1 is 7-smooth run Rader's
+    algorithm (two (n-1)-point FFTs) instead of Chirp-Z; same results as the
+    oracle's Chirp-Z (src/chirpz.rs) within the tolerances, every method, and
+    the same as this library's Chirp-Z path (the default)."""
     import os
 
-    p = cg.CFft1D.with_len(n, dt)
+    os.environ["CHFFT_RADER"] = "1"
+    try:
+        p = cg.CFft1D.with_len(n, dt)
+    finally:
+        os.environ.pop("CHFFT_RADER", None)
     info = p.info()
     if dt == np.float64 and n >= 7681:
         assert info.algorithm in (1, 3)  # tile and staged row do not fit a CTA in f64: Chirp-Z
@@ -354,10 +358,6 @@ def test_rader_lengths(n, dt):
     y = x.copy()
     p.forward0i(y[0])
     close(y[0], oracle.cfft1d(xd[0], "forward0"), dt)
-    os.environ["CHFFT_RADER"] = "0"
-    try:
-        q = cg.CFft1D.with_len(n, dt)
-        assert q.info().algorithm in (1, 3)
-        close(q.execute_batch("forward", x), p.execute_batch("forward", x).astype(np.complex128), dt)
-    finally:
-        os.environ.pop("CHFFT_RADER", None)
+    q = cg.CFft1D.with_len(n, dt)
+    assert q.info().algorithm in (1, 3)
+    close(q.execute_batch("forward", x), p.execute_batch("forward", x).astype(np.complex128), dt)

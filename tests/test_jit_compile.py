@@ -64,6 +64,8 @@ CASES = [
     ("&chfft::kern::k_rows_bb<float, chfft::StatCore<false,true,true,512,512,8,546,16,256,4,0,16,16,2>, 3>", True),
     # Rader rows of N = 1009 (the 1008-point core, one sequence per CTA)
     ("&chfft::kern::k_c2c_rader<float, chfft::StatCore<false,false,true,1008,1008,1,1071,16,352,2,0,16,3,3,7>>", True),
+    # ... and its two-pass order (1008 = 28 x 36), six sequences per CTA
+    ("&chfft::kern::k_c2c_rader<float, chfft::StatCore<false,false,true,1008,1008,6,1045,28,224,2,0,28,36>>", True),
     ("&chfft::kern::k_rows_bb<double, chfft::StatCore<false,true,false,256,256,4,274,16,256,1,0,16,16>, 7>", False),
 ]
 
