@@ -61,6 +61,8 @@ class PlanInfo(ctypes.Structure):
         ("npass", ctypes.c_int), ("radix", ctypes.c_int * 24),
         ("seq_per_cta", ctypes.c_int), ("threads_per_cta", ctypes.c_int), ("smem_per_cta", ctypes.c_size_t),
         ("in_elems", ctypes.c_size_t), ("out_elems", ctypes.c_size_t), ("device_bytes", ctypes.c_size_t),
+        ("cluster_ctas", ctypes.c_int), ("cluster_n1", ctypes.c_size_t), ("cluster_n2", ctypes.c_size_t),
+        ("cluster_max_batch", ctypes.c_size_t),
     ]
 
 

@@ -283,7 +283,11 @@ int chfft_plan_get_info(chfft_plan plan, chfft_plan_info* info) {
   info->in_elems = p.in_elems(false);
   info->out_elems = p.out_elems(false);
   info->device_bytes = p.core.device_bytes() + p.core2.device_bytes() + p.big.device_bytes() + p.work.bytes +
-                       p.aux0.bytes + p.aux1.bytes + p.rader.device_bytes();
+                       p.aux0.bytes + p.aux1.bytes + p.rader.device_bytes() + p.clus.device_bytes();
+  info->cluster_ctas = p.clus.n ? p.clus.csize : 0;
+  info->cluster_n1 = p.clus.n ? (size_t)p.clus.n1 : 0;
+  info->cluster_n2 = p.clus.n ? (size_t)p.clus.n2 : 0;
+  info->cluster_max_batch = p.clus.n ? (size_t)p.clus.max_batch : 0;
   return CHFFT_OK;
 }
 

@@ -1,0 +1,25 @@
+// Host interface of the cluster latency form (k_cluster.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+namespace chfft {
+namespace clus {
+struct ClusterArgs;
+}
+
+// One launch: `batch` transforms, one cluster of `csize` CTAs (8 or 16) each.
+cudaError_t cluster_launch(int dtype, const clus::ClusterArgs& a, long long batch, int csize, int threads,
+                           size_t smem, cudaStream_t s);
+// Per-pass input twiddles of a cluster FFT of length n (pass radices in
+// `code`, 4 bits each): rows 1 .. np - 1, n entries each, into out.
+cudaError_t cluster_pass_tables(int dtype, int n, unsigned long long code, int np, void* out, cudaStream_t s);
+// The four-step twiddles w_n^(n2 k1) x scale at n2 * n1 + k1.
+cudaError_t cluster_block_table(int dtype, long long n, int n1, double scale, void* out, cudaStream_t s);
+// Clusters of this shape the current device can hold at once (0: none, the
+// shape cannot launch).
+int cluster_max_active(int dtype, int csize, int threads, size_t smem);
+
+}  // namespace chfft

@@ -17,6 +17,8 @@
 
 #include "../../include/chfft_gpu.h"
 #include "jit.hpp"
+#include "cluster.hpp"
+#include "k_cluster.cuh"
 #include "k_pipe.cuh"
 #include "pipe.hpp"
 
@@ -845,6 +847,167 @@ void BigCore::exec(const void* in, void* out, void* work, long long batch, bool 
       pass_b(2, tmp, dst, n, back);         // conj(.) c, k < n
     }
   }
+}
+
+// ---------------------------------------------------------------- cluster latency form
+
+namespace {
+// Radix passes of the cluster kernels for a 7-smooth n: radix 4 while
+// possible, then 2, 3, 5, 7 (compact bodies: the launch is bound by
+// instruction fetch, so few distinct radices). false: not 7-smooth or more
+// than 16 passes.
+bool cluster_code(long long n, unsigned long long* code, int* np, int* min_r) {
+  *code = 0;
+  *np = 0;
+  *min_r = 8;
+  auto push = [&](int r) {
+    if (*np >= 16) return false;
+    *code |= (unsigned long long)r << (4 * *np);
+    ++*np;
+    *min_r = std::min(*min_r, r);
+    return true;
+  };
+  while (n % 4 == 0) {
+    if (!push(4)) return false;
+    n /= 4;
+  }
+  for (int r : {2, 3, 5, 7})
+    while (n % r == 0) {
+      if (!push(r)) return false;
+      n /= r;
+    }
+  return n == 1;
+}
+}  // namespace
+
+bool ClusterCore::build(long long n_, int dtype_, cudaStream_t s) {
+  release();
+  // CHFFT_CLUSTER: 0 off, 8 or 16 forces the cluster size (and the form for
+  // f32, whose single-CTA rows are not bound by the arithmetic rate), unset:
+  // f64 only, the size below.
+  int force = 0;
+  if (const char* e = std::getenv("CHFFT_CLUSTER")) {
+    if (e[0] == '0' && e[1] == 0) return false;
+    force = std::atoi(e);
+    if (force != 8 && force != 16) force = 0;
+  }
+  if (dtype_ == 0 && !force) return false;
+  if (n_ < 64 || n_ > (1LL << 20)) return false;
+  const size_t cbytes = cplx_bytes(dtype_);
+  struct Pick {
+    int n1 = 0, n2 = 0, c = 0, th = 0, lda = 0, ldb = 0, tsz = 0, npa = 0, npb = 0;
+    unsigned long long ca = 0, cb = 0;
+    size_t smem = 0;
+    double cost = 0;
+  };
+  // 16 CTAs from 1024 points up (measured on GB300, f64 fwd + bwd device
+  // time: N = 1024 7.3k against 8.1k cycles per launch, N = 4096 20 against
+  // 29 us per pair), 8 below (N = 256: 12 against 14 us).
+  const int order[2] = {n_ >= 1024 ? 16 : 8, n_ >= 1024 ? 8 : 16};
+  for (int c : order) {
+    if (force && c != force) continue;
+    Pick best;
+    for (long long a1 = c; a1 * c <= n_; a1 += c) {
+      if (n_ % a1 || (n_ / a1) % c) continue;
+      const long long a2 = n_ / a1;
+      Pick q;
+      int ra = 0, rb = 0;
+      if (!cluster_code(a1, &q.ca, &q.npa, &ra) || !cluster_code(a2, &q.cb, &q.npb, &rb)) continue;
+      const int wa = (int)(a2 / c), wb = (int)(a1 / c);
+      q.lda = (int)(a1 | 1);
+      q.ldb = (int)(a2 | 1);
+      q.tsz = std::max(wa * q.lda, wb * q.ldb);
+      const size_t tabs = (size_t)(q.npa - 1) * a1 + (size_t)(q.npb - 1) * a2 + (size_t)wa * a1;
+      q.smem = (3 * (size_t)q.tsz + tabs) * cbytes + 2 * clus::kClusterMaxPasses * sizeof(clus::FDiv);
+      if (q.smem > kMaxSmem) continue;
+      // Two threads per element of the CTA's share (n / c), up to the launch bounds.
+      const long long per = 2 * n_ / c;
+      q.th = (int)std::min<long long>(clus::kClusterThreads, std::max<long long>(32, (per + 31) / 32 * 32));
+      // Fewest passes (each a barrier), then the most balanced split.
+      q.cost = q.npa + q.npb + 0.01 * std::fabs(std::log2((double)a1 / (double)a2));
+      q.n1 = (int)a1;
+      q.n2 = (int)a2;
+      q.c = c;
+      if (!best.c || q.cost < best.cost) best = q;
+    }
+    if (!best.c) continue;
+    if (cluster_max_active(dtype_, best.c, best.th, best.smem) <= 0) continue;
+    n = n_;
+    dtype = dtype_;
+    n1 = best.n1;
+    n2 = best.n2;
+    csize = best.c;
+    threads = best.th;
+    lda = best.lda;
+    ldb = best.ldb;
+    tsz = best.tsz;
+    npa = best.npa;
+    npb = best.npb;
+    code_a = best.ca;
+    code_b = best.cb;
+    smem = best.smem;
+    // Batches up to one cluster per csize SMs: every transform's cluster
+    // runs at once (CHFFT_CLUSTER_MAX_BATCH overrides).
+    max_batch = std::max(1, num_sms() / csize);
+    if (const char* e = std::getenv("CHFFT_CLUSTER_MAX_BATCH")) max_batch = std::max(0LL, std::atoll(e));
+    tab_a.ensure(std::max<size_t>(1, (size_t)(npa - 1) * n1) * cbytes);
+    tab_b.ensure(std::max<size_t>(1, (size_t)(npb - 1) * n2) * cbytes);
+    CHFFT_CUDA(cluster_pass_tables(dtype, n1, code_a, npa, tab_a.p, s));
+    CHFFT_CUDA(cluster_pass_tables(dtype, n2, code_b, npb, tab_b.p, s));
+    // The scales of the CFft1D methods, computed as the plan computes them.
+    scales[0] = 1.0;
+    scales[1] = 1.0 / std::sqrt((double)n);
+    scales[2] = 1.0 / (double)n;
+    for (int k = 0; k < kScales; k++) {
+      blk[k].ensure((size_t)n * cbytes);
+      CHFFT_CUDA(cluster_block_table(dtype, n, n1, scales[k], blk[k].p, s));
+    }
+    err.ensure();
+    return true;
+  }
+  return false;
+}
+
+bool ClusterCore::exec(const void* in, void* out, long long batch, bool back, double scale, cudaStream_t s) const {
+  int k = 0;
+  while (k < kScales && scales[k] != scale) k++;
+  if (k == kScales) return false;
+  clus::ClusterArgs a{};
+  a.in = in;
+  a.out = out;
+  a.tab_a = tab_a.p;
+  a.tab_b = tab_b.p;
+  a.blk = blk[k].p;
+  a.dist = n;
+  a.code_a = code_a;
+  a.code_b = code_b;
+  a.npa = npa;
+  a.npb = npb;
+  a.n1 = n1;
+  a.n2 = n2;
+  a.wa = n2 / csize;
+  a.wb = n1 / csize;
+  a.lda = lda;
+  a.ldb = ldb;
+  a.tsz = tsz;
+  // Divisions by each pass's Ns (the product of the earlier radices) and by
+  // the columns / rows per CTA.
+  auto mk_div = [](int d) {
+    clus::FDiv f;
+    f.d = d;
+    f.m = ((1ULL << 40) / (unsigned long long)d) + 1;
+    return f;
+  };
+  for (int pass = 0, ns = 1; pass < npa; ns *= (int)((code_a >> (4 * pass)) & 15), pass++) a.ns_a[pass] = mk_div(ns);
+  for (int pass = 0, ns = 1; pass < npb; ns *= (int)((code_b >> (4 * pass)) & 15), pass++) a.ns_b[pass] = mk_div(ns);
+  a.div_wa = mk_div(n2 / csize);
+  a.div_wb = mk_div(n1 / csize);
+  a.back = back ? 1 : 0;
+  a.err = err.dev;
+  a.spin_limit = spin_limit();
+  a.stall = stall_test();
+  CHFFT_CUDA(cluster_launch(dtype, a, batch, csize, threads, smem, s));
+  return true;
 }
 
 }  // namespace chfft

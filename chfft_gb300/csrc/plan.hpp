@@ -148,6 +148,44 @@ struct RaderCore {
   size_t device_bytes() const { return lc.device_bytes() + perm.bytes + bhat.bytes; }
 };
 
+// Latency form of small CFft1D batches (k_cluster.cuh): one transform per
+// thread-block cluster of csize CTAs, N = n1 x n2 split over the cluster
+// (each CTA n2 / csize columns, then n1 / csize rows), the exchange through
+// distributed shared memory. Built for 7-smooth lengths with such a split;
+// used for batches of at most max_batch transforms.
+struct ClusterCore {
+  long long n = 0;
+  int dtype = 0, n1 = 0, n2 = 0, csize = 0, threads = 0, lda = 0, ldb = 0, tsz = 0;
+  int npa = 0, npb = 0;
+  unsigned long long code_a = 0, code_b = 0;  // radix of pass p at bits [4p, 4p + 4)
+  size_t smem = 0;
+  long long max_batch = 0;
+  DevBuf tab_a, tab_b;  // per-pass input twiddles of the n1- and n2-point FFTs
+  // Four-step twiddles x scale ([n2][k1]) for the scales of the CFft1D
+  // methods: 1, 1 / sqrt(n), 1 / n.
+  static constexpr int kScales = 3;
+  double scales[kScales] = {};
+  DevBuf blk[kScales];
+  // Host-mapped error word: 7 when a CTA's wait for its rows gave up.
+  HostWord err;
+  // false: no split, no cluster shape that launches, or CHFFT_CLUSTER=0.
+  bool build(long long n, int dtype, cudaStream_t s);
+  void release() {
+    n = 0;
+    max_batch = 0;
+    tab_a.release();
+    tab_b.release();
+    for (auto& b : blk) b.release();
+  }
+  // false (nothing launched) for a scale without a table.
+  bool exec(const void* in, void* out, long long batch, bool back, double scale, cudaStream_t s) const;
+  size_t device_bytes() const {
+    size_t b = tab_a.bytes + tab_b.bytes;
+    for (const auto& x : blk) b += x.bytes;
+    return b;
+  }
+};
+
 // Launch geometry of a CTA-per-`tpb`-sequences kernel.
 struct Geo {
   int tpb = 1, threads = 32;
@@ -172,8 +210,9 @@ long long bluestein_length(long long n, int dtype);
 // default 4,000,000 (about a second at ~0.25 us per poll).
 long long spin_limit();
 // Test hook: CHFFT_TEST_STALL=1 makes one dependency of each pipelined
-// four-step launch unreachable, so a bounded wait runs out and the call
-// reports CHFFT_ETIMEOUT (the kernels still return normally).
+// four-step launch, and the rows' arrival wait of each cluster launch,
+// unreachable, so a bounded wait runs out and the call reports
+// CHFFT_ETIMEOUT (the kernels still return normally).
 int stall_test();
 
 // Whether plan-time specialised kernels are used for a launch of `elems`

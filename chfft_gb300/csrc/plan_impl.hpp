@@ -99,6 +99,9 @@ struct PlanImpl {
   // Chirp-Z core for the other paths.
   RaderCore rader;
   bool use_rader = false;
+  // CFft1D batches of at most clus.max_batch transforms: one thread-block
+  // cluster per transform (the latency form; f64 by default).
+  ClusterCore clus;
   PlanOpts opts;         // tuning knobs (chfft_plan_set_config)
   DevBuf work;           // four-step workspace
   DevBuf aux0, aux1;
@@ -153,6 +156,8 @@ struct PlanImpl {
             throw Fail{CHFFT_EUNSUPPORTED, "transform length " + std::to_string(len) + " is not supported"};
           use_big = true;
         }
+        clus.release();
+        if (!use_rader && !(one_cta && core.blue) && !(use_big && big.blue)) clus.build(len, dtype, s);
         break;
       }
       case CHFFT_KIND_CFFT2D:
@@ -319,6 +324,8 @@ struct PlanImpl {
             CHFFT_CUDA(cudaMemcpyAsync(d_out, d_in, batch * cplx_bytes(dtype), cudaMemcpyDeviceToDevice, s));
           return;
         }
+        if (clus.n && batch <= clus.max_batch && opts.tc <= 0 && clus.exec(d_in, d_out, batch, ms.back, sc, s))
+          return;
         if (use_big) {
           work.ensure((size_t)big.work_elems(batch) * cplx_bytes(dtype));
           big.exec(d_in, d_out, work.p, batch, ms.back, sc, s);
@@ -385,6 +392,9 @@ struct PlanImpl {
   void check_waits() {
     if (int code = big.err.take())
       throw Fail{CHFFT_ETIMEOUT, "a device-side wait of the pipelined four-step launch gave up (code " +
+                                     std::to_string(code) + "); that launch's output is incomplete"};
+    if (int code = clus.err.take())
+      throw Fail{CHFFT_ETIMEOUT, "a CTA of the cluster launch gave up waiting for its rows (code " +
                                      std::to_string(code) + "); that launch's output is incomplete"};
   }
 

@@ -231,6 +231,14 @@ typedef struct chfft_plan_info {
   size_t smem_per_cta;
   size_t in_elems, out_elems; /* per transform, in the method's element type (forward direction) */
   size_t device_bytes;        /* tables + workspace held by the plan */
+  /* CFft1D latency form: batches of at most cluster_max_batch transforms run
+   * one transform per thread-block cluster of cluster_ctas CTAs (N =
+   * cluster_n1 x cluster_n2 split over the cluster, exchange through
+   * distributed shared memory); 0 when the plan has none. f64 plans of
+   * 7-smooth lengths from 64 to 2^20 with such a split, f32 plans only with
+   * CHFFT_CLUSTER=8 or 16 at plan creation (CHFFT_CLUSTER=0 turns it off). */
+  int cluster_ctas;
+  size_t cluster_n1, cluster_n2, cluster_max_batch;
 } chfft_plan_info;
 
 CHFFT_API int chfft_plan_get_info(chfft_plan plan, chfft_plan_info* info);

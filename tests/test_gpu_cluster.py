@@ -1,0 +1,168 @@
+"""GPU: the cluster latency form of small CFft1D batches (k_cluster.cuh),
+through the C ABI.
+
+One transform per thread-block cluster of 8 or 16 CTAs, N = n1 x n2 split
+over the cluster, the exchange through distributed shared memory. f64
+plans take it by default for batches up to chfft_plan_info.cluster_max_batch;
+f32 plans only with CHFFT_CLUSTER=8 or 16 at plan creation. Checked against
+the oracle (f64 relative L2 <= 1e-12, f32 <= 5e-6) for every method kind,
+lengths one CTA holds and lengths beyond it, both cluster sizes, batches
+around the threshold, in-place device calls and a captured CUDA graph.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+cg = pytest.importorskip("chfft_gb300")
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+TOL = {np.float64: 1e-12, np.float32: 5e-6}
+CPLX = {np.float64: np.complex128, np.float32: np.complex64}
+
+
+def rel(a, b):
+    a = np.asarray(a, np.complex128)
+    b = np.asarray(b, np.complex128)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+class env:
+    """Temporarily set environment variables (None removes)."""
+
+    def __init__(self, **kv):
+        self.kv = kv
+        self.old = {}
+
+    def __enter__(self):
+        for k, v in self.kv.items():
+            self.old[k] = os.environ.get(k)
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+        return self
+
+    def __exit__(self, *exc):
+        for k, v in self.old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
+def data(batch, n, seed, dt):
+    rng = np.random.default_rng(seed)
+    return (rng.uniform(-1, 1, (batch, n)) + 1j * rng.uniform(-1, 1, (batch, n))).astype(CPLX[dt])
+
+
+def plan(n, dt, size=None):
+    with env(CHFFT_CLUSTER=size):
+        p = cg.CFft1D.with_len(n, dt)
+    return p
+
+
+F64_LENGTHS = [64, 256, 1024, 2304, 4096, 16384]
+
+
+@pytest.mark.parametrize("n", F64_LENGTHS)
+def test_f64_default_takes_cluster_and_matches_oracle(n):
+    p = plan(n, np.float64)
+    info = p.info()
+    assert info.cluster_ctas in (8, 16)
+    assert info.cluster_n1 * info.cluster_n2 == n
+    assert info.cluster_max_batch >= 1
+    x = data(2, n, n, np.float64)
+    for b in (1, 2):
+        y = p.execute_batch("forward", x[:b])
+        for i in range(b):
+            assert rel(y[i], oracle.cfft1d(x[i], "forward")) <= 1e-12
+    z = p.execute_batch("backward", y)
+    assert rel(z, x) <= 1e-12
+    assert rel(p.execute_batch("forwardu", x), np.fft.fft(x, axis=-1) / np.sqrt(n)) <= 1e-12
+    assert rel(p.execute_batch("backward0", y), x * n) <= 1e-12
+
+
+@pytest.mark.parametrize("size", ["8", "16"])
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+@pytest.mark.parametrize("n", [1024, 4096, 16384])
+def test_forced_cluster_sizes(size, dt, n):
+    p = plan(n, dt, size)
+    info = p.info()
+    if info.cluster_ctas == 0:
+        pytest.skip(f"no {size}-CTA split of {n} within the shape limits")
+    assert info.cluster_ctas == int(size)
+    x = data(3, n, 7, dt)
+    y = p.execute_batch("forward", x)
+    assert rel(y, np.fft.fft(x.astype(np.complex128), axis=-1)) <= TOL[dt]
+    assert rel(p.execute_batch("backward", y), x) <= TOL[dt] * 2
+
+
+def test_threshold_batches_agree_with_row_path():
+    """Batches at and just above cluster_max_batch (the second runs the
+    one-CTA-per-transform rows) give the same spectra."""
+    n = 1024
+    p = plan(n, np.float64)
+    mb = p.info().cluster_max_batch
+    x = data(mb + 1, n, 5, np.float64)
+    ref = np.fft.fft(x, axis=-1)
+    assert rel(p.execute_batch("forward", x[:mb]), ref[:mb]) <= 1e-12
+    assert rel(p.execute_batch("forward", x), ref) <= 1e-12
+    off = plan(n, np.float64, "0")
+    assert off.info().cluster_ctas == 0
+    assert rel(off.execute_batch("forward", x[:1]), ref[:1]) <= 1e-12
+
+
+def test_max_batch_override_and_in_place_device():
+    n, batch = 4096, 40
+    with env(CHFFT_CLUSTER_MAX_BATCH="64"):
+        p = cg.CFft1D.with_len(n, np.float64)
+    assert p.info().cluster_max_batch == 64
+    x = data(batch, n, 9, np.float64)
+    ref = np.fft.fft(x, axis=-1)
+    s = torch.cuda.current_stream().cuda_stream
+    d = torch.from_numpy(x.view(np.float64)).cuda()
+    p.execute_device("forward0i", d.data_ptr(), d.data_ptr(), batch, s)  # in place
+    p.wait(s)
+    assert rel(d.cpu().numpy().view(np.complex128), ref) <= 1e-12
+
+
+def test_graph_capture_replays():
+    n = 1024
+    p = plan(n, np.float64)
+    x = data(1, n, 3, np.float64)
+    dev = torch.device("cuda", 0)
+    d_x = torch.from_numpy(x.view(np.float64)).to(dev)
+    d_y = torch.empty_like(d_x)
+    d_z = torch.empty_like(d_x)
+    p.execute_device("forward", d_x.data_ptr(), d_y.data_ptr(), 1, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        sp = torch.cuda.current_stream().cuda_stream
+        p.execute_device("forward", d_x.data_ptr(), d_y.data_ptr(), 1, sp)
+        p.execute_device("backward", d_y.data_ptr(), d_z.data_ptr(), 1, sp)
+    for _ in range(3):
+        g.replay()
+    torch.cuda.synchronize()
+    assert rel(d_y.cpu().numpy().view(np.complex128), oracle.cfft1d(x[0], "forward")) <= 1e-12
+    assert rel(d_z.cpu().numpy().view(np.complex128), x) <= 1e-12
+
+
+def test_cluster_bounded_wait_runs_out_and_recovers():
+    """Rows waiting for bytes that never come: the bounded wait gives up, the
+    launch returns, the call reports CHFFT_ETIMEOUT; the next call is correct."""
+    n = 1024
+    p = plan(n, np.float64)
+    assert p.info().cluster_ctas
+    x = data(1, n, 4, np.float64)
+    with env(CHFFT_TEST_STALL="1", CHFFT_SPIN_LIMIT="2000"):
+        with pytest.raises(cg.ChfftError) as e:
+            p.execute_batch("forward", x)
+        assert e.value.status == cg.ETIMEOUT
+    p.wait(0)
+    assert rel(p.execute_batch("forward", x), np.fft.fft(x, axis=-1)) <= 1e-12
