@@ -10,8 +10,12 @@ namespace clus {
 struct ClusterArgs;
 }
 
-// One launch: `batch` transforms, one cluster of `csize` CTAs (8 or 16) each.
-cudaError_t cluster_launch(int dtype, const clus::ClusterArgs& a, long long batch, int csize, int threads,
+// The kernel for a split: the compile-time-shape instance of (n1, n2,
+// csize) when there is one (its thread count into *threads; CHFFT_CLUSTER_STATIC=0
+// skips them), else the run-time-shape kernel (*threads unchanged).
+const void* cluster_kernel(int dtype, int n1, int n2, int csize, int* threads);
+// One launch of kernel fn: `batch` transforms, one cluster of `csize` CTAs (8 or 16) each.
+cudaError_t cluster_launch(const void* fn, const clus::ClusterArgs& a, long long batch, int csize, int threads,
                            size_t smem, cudaStream_t s);
 // Per-pass input twiddles of a cluster FFT of length n (pass radices in
 // `code`, 4 bits each): rows 1 .. np - 1, n entries each, into out.
@@ -20,6 +24,6 @@ cudaError_t cluster_pass_tables(int dtype, int n, unsigned long long code, int n
 cudaError_t cluster_block_table(int dtype, long long n, int n1, double scale, void* out, cudaStream_t s);
 // Clusters of this shape the current device can hold at once (0: none, the
 // shape cannot launch).
-int cluster_max_active(int dtype, int csize, int threads, size_t smem);
+int cluster_max_active(const void* fn, int csize, int threads, size_t smem);
 
 }  // namespace chfft

@@ -1,5 +1,12 @@
-// Host side of the cluster latency form (k_cluster.cuh): the launch with a
-// cluster-dimension attribute and the per-device function attributes.
+// Host side of the cluster latency form (k_cluster.cuh): the kernel choice
+// (a compile-time-shape instance for the power-of-two splits, else the
+// run-time-shape kernel), the launch with a cluster-dimension attribute,
+// the per-device function attributes and the plan-time tables.
+#include <cstdlib>
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "cluster.hpp"
 #include "k_cluster.cuh"
 
@@ -8,72 +15,64 @@ namespace {
 
 constexpr int kPasses = clus::kClusterMaxPasses;
 
-template <typename T>
-cudaError_t prepare(int csize, size_t smem) {
-  // Function attributes are per device: set once per device and size.
-  static int done_smem[64] = {0};
-  static int done_np[64] = {0};
+using ClusterFn = void (*)(const clus::ClusterArgs);
+
+// Function attributes are per device: the dynamic shared-memory size and
+// (clusters of more than 8 CTAs) the non-portable cluster size, set once
+// per (kernel, device) and size.
+cudaError_t prepare(const void* fn, int csize, size_t smem) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, std::pair<size_t, bool>> done;
   int dev = 0;
-  cudaGetDevice(&dev);
-  auto fn = clus::k_c2c_cluster<T>;
-  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  if (smem > 48 * 1024 && done_smem[dev] < (int)smem) {
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> g(mu);
+  auto& d = done[{fn, dev}];
+  if (smem > 48 * 1024 && d.first < smem) {
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    done_smem[dev] = (int)smem;
+    d.first = smem;
   }
-  if (csize > 8 && !done_np[dev]) {
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (csize > 8 && !d.second) {
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
-    done_np[dev] = 1;
+    d.second = true;
   }
   return cudaSuccess;
 }
 
-template <typename T>
-cudaError_t launch_t(const clus::ClusterArgs& a, long long batch, int csize, int threads, size_t smem,
-                     cudaStream_t s) {
-  cudaError_t e = prepare<T>(csize, smem);
-  if (e != cudaSuccess) return e;
-  cudaLaunchConfig_t cfg{};
-  cfg.gridDim = dim3((unsigned)(batch * csize), 1, 1);
-  cfg.blockDim = dim3((unsigned)threads, 1, 1);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cudaLaunchAttribute at[1];
+void cluster_config(cudaLaunchConfig_t* cfg, cudaLaunchAttribute* at, long long batch, int csize, int threads,
+                    size_t smem, cudaStream_t s) {
+  *cfg = cudaLaunchConfig_t{};
+  cfg->gridDim = dim3((unsigned)(batch * csize), 1, 1);
+  cfg->blockDim = dim3((unsigned)threads, 1, 1);
+  cfg->dynamicSmemBytes = smem;
+  cfg->stream = s;
   at[0].id = cudaLaunchAttributeClusterDimension;
   at[0].val.clusterDim.x = (unsigned)csize;
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, clus::k_c2c_cluster<T>, a);
+  cfg->attrs = at;
+  cfg->numAttrs = 1;
 }
 
-template <typename T>
-int max_clusters_t(int csize, int threads, size_t smem) {
-  if (prepare<T>(csize, smem) != cudaSuccess) {
-    cudaGetLastError();
-    return 0;
+struct StaticInst {
+  int n1, n2, cs, threads;
+  ClusterFn f32, f64;
+};
+#define CHFFT_CLUSTER_INST(A, B, CS)                                                                      \
+  StaticInst {                                                                                          \
+    A, B, CS, clus::CShape<A, B, CS>::THREADS, clus::k_c2c_cluster_s<float, A, B, CS>,                  \
+        clus::k_c2c_cluster_s<double, A, B, CS>                                                         \
   }
-  cudaLaunchConfig_t cfg{};
-  cfg.gridDim = dim3((unsigned)csize, 1, 1);
-  cfg.blockDim = dim3((unsigned)threads, 1, 1);
-  cfg.dynamicSmemBytes = smem;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = (unsigned)csize;
-  at[0].val.clusterDim.y = 1;
-  at[0].val.clusterDim.z = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  int n = 0;
-  if (cudaOccupancyMaxActiveClusters(&n, clus::k_c2c_cluster<T>, &cfg) != cudaSuccess) {
-    cudaGetLastError();
-    return 0;
-  }
-  return n;
-}
+// The splits the plans pick for N = 2^6 .. 2^14 (fewest passes, then the
+// most balanced; 8 CTAs below 1024 points, 16 from there).
+const StaticInst kStatic[] = {
+    CHFFT_CLUSTER_INST(8, 8, 8),     CHFFT_CLUSTER_INST(8, 16, 8),    CHFFT_CLUSTER_INST(16, 16, 8),
+    CHFFT_CLUSTER_INST(16, 32, 8),   CHFFT_CLUSTER_INST(16, 64, 16),  CHFFT_CLUSTER_INST(32, 64, 16),
+    CHFFT_CLUSTER_INST(64, 64, 16),  CHFFT_CLUSTER_INST(64, 128, 16), CHFFT_CLUSTER_INST(128, 128, 16),
+};
+#undef CHFFT_CLUSTER_INST
 
 // exp(-2 pi i e / n) in FP64 for 0 <= e < n, the numerator reduced to
 // (-n/2, n/2] so the sincospi argument stays small.
@@ -147,14 +146,41 @@ cudaError_t cluster_block_table(int dtype, long long n, int n1, double scale, vo
   return cudaGetLastError();
 }
 
-cudaError_t cluster_launch(int dtype, const clus::ClusterArgs& a, long long batch, int csize, int threads,
-                           size_t smem, cudaStream_t s) {
-  return dtype == 0 ? launch_t<float>(a, batch, csize, threads, smem, s)
-                    : launch_t<double>(a, batch, csize, threads, smem, s);
+const void* cluster_kernel(int dtype, int n1, int n2, int csize, int* threads) {
+  const char* e = std::getenv("CHFFT_CLUSTER_STATIC");
+  if (!(e && e[0] == '0'))
+    for (const auto& k : kStatic)
+      if (k.n1 == n1 && k.n2 == n2 && k.cs == csize) {
+        *threads = k.threads;
+        return reinterpret_cast<const void*>(dtype == 0 ? k.f32 : k.f64);
+      }
+  return reinterpret_cast<const void*>(dtype == 0 ? clus::k_c2c_cluster<float> : clus::k_c2c_cluster<double>);
 }
 
-int cluster_max_active(int dtype, int csize, int threads, size_t smem) {
-  return dtype == 0 ? max_clusters_t<float>(csize, threads, smem) : max_clusters_t<double>(csize, threads, smem);
+cudaError_t cluster_launch(const void* fn, const clus::ClusterArgs& a, long long batch, int csize, int threads,
+                           size_t smem, cudaStream_t s) {
+  cudaError_t e = prepare(fn, csize, smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg;
+  cudaLaunchAttribute at[1];
+  cluster_config(&cfg, at, batch, csize, threads, smem, s);
+  return cudaLaunchKernelEx(&cfg, reinterpret_cast<ClusterFn>(const_cast<void*>(fn)), a);
+}
+
+int cluster_max_active(const void* fn, int csize, int threads, size_t smem) {
+  if (prepare(fn, csize, smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  cudaLaunchConfig_t cfg;
+  cudaLaunchAttribute at[1];
+  cluster_config(&cfg, at, 1, csize, threads, smem, nullptr);
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, fn, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
 }
 
 }  // namespace chfft

@@ -396,5 +396,167 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_c2c_cluster(const Cluste
   }
 }
 
+// ---------------------------------------------------------------------------
+// The same kernel with the split fixed at compile time, for the power-of-two
+// splits the plans pick (N = 64 .. 16384): every division, stride and pass
+// radix is a constant, the passes are straight-line code and each thread's
+// items of a pass are unrolled together, so the index arithmetic that
+// dominates the run-time-shape kernel's pass latency folds away. Shared
+// memory layout, tables and arguments are the run-time kernel's.
+CHFFT_HD constexpr int pow2_passes(int n) {  // radix 4 while possible, then 2
+  int p = 0;
+  while (n % 4 == 0) {
+    n /= 4;
+    p++;
+  }
+  return n == 2 ? p + 1 : p;
+}
+CHFFT_HD constexpr int pow2_radix(int n, int p) {
+  int q4 = 0;
+  while (n % 4 == 0) {
+    n /= 4;
+    q4++;
+  }
+  return p < q4 ? 4 : 2;
+}
+CHFFT_HD constexpr int pow2_ns(int n, int p) {
+  int s = 1;
+  for (int i = 0; i < p; i++) s *= pow2_radix(n, i);
+  return s;
+}
+
+template <int N1, int N2, int CS>
+struct CShape {
+  static constexpr int WA = N2 / CS, WB = N1 / CS;
+  static constexpr int LDA = N1 | 1, LDB = N2 | 1;
+  static constexpr int TSZ = WA * LDA > WB * LDB ? WA * LDA : WB * LDB;
+  static constexpr int E = N1 * WA;  // elements per CTA in either phase
+  static constexpr int THREADS = 2 * E < 32 ? 32 : (2 * E > kClusterThreads ? kClusterThreads : 2 * E);
+  static constexpr int NPA = pow2_passes(N1), NPB = pow2_passes(N2);
+  static_assert(N1 % CS == 0 && N2 % CS == 0, "split not divisible by the cluster size");
+};
+
+// One compile-time radix-R pass: ITEMS = 2 TPB N work items over THREADS
+// threads, every thread running every trip (the pair shuffle sees full
+// warps), a trip's items unrolled together.
+template <int R, int NS, int N, int TPB, int LD, int OUT, int THREADS, int WB, int LDB, int N1, typename C>
+__device__ __forceinline__ void spass(const C* src, C* dst, const C* tw, const ClusterArgs& a, int col0, C* out,
+                                      unsigned long long* bar) {
+  using Rl = typename Real<C>::type;
+  constexpr int NB = N / R, ITEMS = 2 * TPB * N, TRIPS = (ITEMS + THREADS - 1) / THREADS;
+  const int h = threadIdx.x & 1;
+#pragma unroll
+  for (int it = 0; it < TRIPS; it++) {
+    const int w = it * THREADS + threadIdx.x;
+    const bool act = ITEMS % THREADS == 0 || w < ITEMS;
+    const int e = act ? w >> 1 : 0;
+    const int pos = e / TPB, t = e % TPB;
+    const int u = pos / NS, jm = pos % NS;
+    const int q = u / R, k = u % R;
+    const C* s = src + t * LD + q * NS + jm;
+    C v[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) v[r] = s[r * NB];
+    const Rl x = dft_part<R>(v, k, h);
+    if constexpr (OUT == kToGlobal) {
+      if (act) reinterpret_cast<Rl*>(out)[2 * (t + N1 * pos) + h] = flip_if(x, a.back && h);
+    } else {
+      const Rl other = __shfl_xor_sync(0xffffffffu, x, 1);
+      const C wv = OUT == kToSmemNext ? tw[pos] : tw[t * N + pos];
+      const Rl y = fma(x, wv.x, flip_if(other * wv.y, h == 0));
+      if constexpr (OUT == kToSmemNext) {
+        if (act) reinterpret_cast<Rl*>(dst)[2 * (t * LD + pos) + h] = y;
+      } else {
+        const int owner = pos / WB, tb = pos % WB;
+        const unsigned la = su32(reinterpret_cast<Rl*>(dst) + 2 * (tb * LDB + col0 + t) + h);
+        if (act) st_async(peer_u32(la, (unsigned)owner), y, peer_u32(su32(bar), (unsigned)owner));
+      }
+    }
+  }
+}
+
+template <int P, class S, int N1, int N2, typename C>
+__device__ __forceinline__ void scols(C* src, C* dst, C* buf2, const C* sta, const C* sblk, const ClusterArgs& a,
+                                      int col0, unsigned long long* bar) {
+  constexpr int R = pow2_radix(N1, P), NS = pow2_ns(N1, P);
+  if constexpr (P + 1 < S::NPA) {
+    spass<R, NS, N1, S::WA, S::LDA, kToSmemNext, S::THREADS, S::WB, S::LDB, N1>(src, dst, sta + P * N1, a, col0,
+                                                                             (C*)nullptr, bar);
+    __syncthreads();
+    scols<P + 1, S, N1, N2>(dst, src, buf2, sta, sblk, a, col0, bar);
+  } else {
+    cluster_wait();  // every CTA of the cluster has started
+    spass<R, NS, N1, S::WA, S::LDA, kToPeers, S::THREADS, S::WB, S::LDB, N1>(src, buf2, sblk, a, col0, (C*)nullptr,
+                                                                          bar);
+  }
+}
+
+template <int P, class S, int N1, int N2, typename C>
+__device__ __forceinline__ void srows(C* src, C* dst, C* other, const C* stb, const ClusterArgs& a, C* out) {
+  constexpr int R = pow2_radix(N2, P), NS = pow2_ns(N2, P);
+  if constexpr (P + 1 < S::NPB) {
+    spass<R, NS, N2, S::WB, S::LDB, kToSmemNext, S::THREADS, S::WB, S::LDB, N1>(src, dst, stb + P * N2, a, 0, out,
+                                                                             nullptr);
+    __syncthreads();
+    srows<P + 1, S, N1, N2>(dst, other, dst, stb, a, out);
+  } else {
+    spass<R, NS, N2, S::WB, S::LDB, kToGlobal, S::THREADS, S::WB, S::LDB, N1>(src, dst, stb, a, 0, out, nullptr);
+  }
+}
+
+template <typename T, int N1, int N2, int CS>
+__global__ void __launch_bounds__(CShape<N1, N2, CS>::THREADS, 1) k_c2c_cluster_s(const ClusterArgs a) {
+  using C = cx_t<T>;
+  using S = CShape<N1, N2, CS>;
+  constexpr int TA = (S::NPA - 1) * N1, TB = (S::NPB - 1) * N2, BLK = S::WA * N1, NTAB = TA + TB + BLK;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) unsigned long long arrived;
+  if (threadIdx.x == 0) {
+    mbar_init(&arrived, 1);
+    mbar_arrive_expect(&arrived, (unsigned)(S::WB * N2 * sizeof(C)) + (a.stall ? 16u : 0u));
+  }
+  cluster_arrive();
+  const unsigned c = cluster_rank();
+  const long long tr = blockIdx.x / CS;
+  C* buf0 = reinterpret_cast<C*>(smem_raw);
+  C* buf1 = buf0 + S::TSZ;
+  C* buf2 = buf1 + S::TSZ;
+  C* sta = buf2 + S::TSZ;
+  C* stb = sta + TA;
+  C* sblk = stb + TB;
+  {
+    const C* ga = static_cast<const C*>(a.tab_a);
+    const C* gb = static_cast<const C*>(a.tab_b);
+    const C* gk = static_cast<const C*>(a.blk) + (size_t)c * BLK;
+    const C* in = static_cast<const C*>(a.in) + tr * a.dist + (long long)c * S::WA;
+    constexpr int STEPS = (S::E > NTAB ? S::E : NTAB), TRIPS = (STEPS + S::THREADS - 1) / S::THREADS;
+    C v[TRIPS], w[TRIPS];
+#pragma unroll
+    for (int u = 0; u < TRIPS; u++) {
+      const int b = u * S::THREADS + threadIdx.x;
+      if (b < S::E) v[u] = in[(long long)(b / S::WA) * N2 + b % S::WA];
+      if (b < NTAB) w[u] = b < TA ? ga[b] : b < TA + TB ? gb[b - TA] : gk[b - TA - TB];
+    }
+#pragma unroll
+    for (int u = 0; u < TRIPS; u++) {
+      const int b = u * S::THREADS + threadIdx.x;
+      if (b < S::E) buf0[(b % S::WA) * S::LDA + b / S::WA] = conj_if(v[u], a.back != 0);
+      if (b < NTAB) sta[b] = w[u];
+    }
+  }
+  __syncthreads();
+  scols<0, S, N1, N2>(buf0, buf1, buf2, sta, sblk, a, (int)c * S::WA, &arrived);
+  for (long long i = 0; !mbar_test(&arrived, 0); i++) {
+    if (i >= a.spin_limit) {
+      if (a.err && threadIdx.x == 0) {
+        *(volatile int*)a.err = 7;
+        __threadfence_system();
+      }
+      break;
+    }
+  }
+  srows<0, S, N1, N2>(buf2, buf0, buf1, stb, a, static_cast<C*>(a.out) + tr * a.dist + (int)c * S::WB);
+}
+
 }  // namespace clus
 }  // namespace chfft

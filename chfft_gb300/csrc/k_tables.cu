@@ -92,11 +92,6 @@ __global__ void k_gen(int which, long long n, long long count, long long m, void
       root((long long)(((unsigned long long)k * (unsigned long long)m) % (unsigned long long)n), n, &c, &s);
       put<C>(out, k, c, s);
       break;
-    case Table::FOURSTEP:
-      root((long long)(((unsigned long long)(k / m) * (unsigned long long)(k % m)) % (unsigned long long)n), n, &c,
-           &s);
-      put<C>(out, k, c, s);
-      break;
   }
 }
 

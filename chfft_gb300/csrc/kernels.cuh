@@ -112,8 +112,7 @@ enum class Table : int {
   VORBIS_WIN = 8,  // real: sin(pi/2 sin^2(pi (k + 1/2) / n))
   BLUE_B = 9,      // f64 only: Bluestein kernel sequence for user length n, padded length m, x 1/m
   CHIRP_INDEX = 10,// u64: k*k mod 2n
-  OMEGA_STRIDE = 11,// out[k] = exp(-2 pi i (k*m mod n) / n)
-  FOURSTEP = 12     // out[k] = exp(-2 pi i ((k / m) (k mod m) mod n) / n): rows k1, columns n2 < m
+  OMEGA_STRIDE = 11 // out[k] = exp(-2 pi i (k*m mod n) / n)
 };
 
 template <typename T>

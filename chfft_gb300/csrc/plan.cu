@@ -931,7 +931,9 @@ bool ClusterCore::build(long long n_, int dtype_, cudaStream_t s) {
       if (!best.c || q.cost < best.cost) best = q;
     }
     if (!best.c) continue;
-    if (cluster_max_active(dtype_, best.c, best.th, best.smem) <= 0) continue;
+    const void* k = cluster_kernel(dtype_, best.n1, best.n2, best.c, &best.th);
+    if (cluster_max_active(k, best.c, best.th, best.smem) <= 0) continue;
+    fn = k;
     n = n_;
     dtype = dtype_;
     n1 = best.n1;
@@ -1006,7 +1008,7 @@ bool ClusterCore::exec(const void* in, void* out, long long batch, bool back, do
   a.err = err.dev;
   a.spin_limit = spin_limit();
   a.stall = stall_test();
-  CHFFT_CUDA(cluster_launch(dtype, a, batch, csize, threads, smem, s));
+  CHFFT_CUDA(cluster_launch(fn, a, batch, csize, threads, smem, s));
   return true;
 }
 

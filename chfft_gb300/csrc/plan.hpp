@@ -160,6 +160,7 @@ struct ClusterCore {
   unsigned long long code_a = 0, code_b = 0;  // radix of pass p at bits [4p, 4p + 4)
   size_t smem = 0;
   long long max_batch = 0;
+  const void* fn = nullptr;  // the kernel (compile-time-shape instance or the run-time-shape one)
   DevBuf tab_a, tab_b;  // per-pass input twiddles of the n1- and n2-point FFTs
   // Four-step twiddles x scale ([n2][k1]) for the scales of the CFft1D
   // methods: 1, 1 / sqrt(n), 1 / n.

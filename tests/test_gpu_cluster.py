@@ -166,3 +166,19 @@ def test_cluster_bounded_wait_runs_out_and_recovers():
         assert e.value.status == cg.ETIMEOUT
     p.wait(0)
     assert rel(p.execute_batch("forward", x), np.fft.fft(x, axis=-1)) <= 1e-12
+
+
+@pytest.mark.parametrize("static", ["1", "0"])
+@pytest.mark.parametrize("n", [64, 128, 256, 512, 1024, 2048, 4096, 8192, 16384])
+def test_compile_time_and_run_time_shapes_agree(n, static):
+    """Power-of-two lengths run a compile-time-shape instance of the split;
+    CHFFT_CLUSTER_STATIC=0 runs the run-time-shape kernel instead: both
+    match the FP64 reference, forward and backward, batches 1 and 3."""
+    with env(CHFFT_CLUSTER_STATIC=static):
+        p = cg.CFft1D.with_len(n, np.float64)
+    assert p.info().cluster_ctas in (8, 16)
+    x = data(3, n, n + 1, np.float64)
+    for b in (1, 3):
+        y = p.execute_batch("forward", x[:b])
+        assert rel(y, np.fft.fft(x[:b], axis=-1)) <= 1e-12
+        assert rel(p.execute_batch("backward", y), x[:b]) <= 1e-12
