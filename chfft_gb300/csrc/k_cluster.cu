@@ -52,8 +52,13 @@ void cluster_config(cudaLaunchConfig_t* cfg, cudaLaunchAttribute* at, long long 
   at[0].val.clusterDim.x = (unsigned)csize;
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
+  // Programmatic dependent launch: the kernels wait for their prerequisites
+  // before reading the input (k_cluster.cuh), so this launch may begin
+  // while the previous kernel on the stream finishes.
+  at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[1].val.programmaticStreamSerializationAllowed = 1;
   cfg->attrs = at;
-  cfg->numAttrs = 1;
+  cfg->numAttrs = 2;
 }
 
 struct StaticInst {
@@ -162,7 +167,7 @@ cudaError_t cluster_launch(const void* fn, const clus::ClusterArgs& a, long long
   cudaError_t e = prepare(fn, csize, smem);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg;
-  cudaLaunchAttribute at[1];
+  cudaLaunchAttribute at[2];
   cluster_config(&cfg, at, batch, csize, threads, smem, s);
   return cudaLaunchKernelEx(&cfg, reinterpret_cast<ClusterFn>(const_cast<void*>(fn)), a);
 }
@@ -173,7 +178,7 @@ int cluster_max_active(const void* fn, int csize, int threads, size_t smem) {
     return 0;
   }
   cudaLaunchConfig_t cfg;
-  cudaLaunchAttribute at[1];
+  cudaLaunchAttribute at[2];
   cluster_config(&cfg, at, 1, csize, threads, smem, nullptr);
   int n = 0;
   if (cudaOccupancyMaxActiveClusters(&n, fn, &cfg) != cudaSuccess) {

@@ -58,6 +58,11 @@ __device__ __forceinline__ P* peer(P* local, unsigned rank) {
   asm volatile("mapa.u64 %0, %1, %2;" : "=l"(out) : "l"(reinterpret_cast<unsigned long long>(local)), "r"(rank));
   return reinterpret_cast<P*>(out);
 }
+// Programmatic dependent launch: the next kernel on the stream may start
+// its prologue now; this kernel's reads of memory an earlier kernel wrote
+// wait for that kernel's completion (no-ops without the launch attribute).
+__device__ __forceinline__ void allow_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void wait_prerequisites() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ unsigned su32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 // Shared::cluster address of the same location in CTA `rank`.
 __device__ __forceinline__ unsigned peer_u32(unsigned local, unsigned rank) {
@@ -282,7 +287,10 @@ __device__ __forceinline__ void epass_r(int R, const PassGeo& g, const FDiv& ns,
 // first two; the third receives this CTA's rows from every CTA's last
 // column pass, and the rows ping-pong it with the first), the per-pass
 // twiddle tables of both FFTs, this CTA's four-step block, then the
-// per-pass divisions. Synchronisation: each CTA initialises its arrival
+// per-pass divisions. Launched with programmatic stream serialisation: the
+// next kernel's CTAs may start while this one runs, and every read of the
+// input waits for the kernels before it (griddepcontrol). Synchronisation:
+// each CTA initialises its arrival
 // mbarrier (one arrival expecting its rows' bytes) and arrives on the
 // cluster barrier at entry; the barrier is waited for before the first
 // remote store (every CTA of the cluster has started and initialised its
@@ -298,6 +306,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_c2c_cluster(const Cluste
     mbar_init(&arrived, 1);
     mbar_arrive_expect(&arrived, (unsigned)(a.wb * a.n2 * sizeof(C)) + (a.stall ? 16u : 0u));
   }
+  allow_dependents();
   cluster_arrive();
   const unsigned c = cluster_rank();
   const long long tr = blockIdx.x / cluster_size();
@@ -323,6 +332,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_c2c_cluster(const Cluste
     const C* in = static_cast<const C*>(a.in) + tr * a.dist + (long long)c * wa;
     const int tot = n1 * wa;
     const int steps = max(tot, ntab);
+    wait_prerequisites();
     for (int b0 = threadIdx.x; b0 < steps; b0 += kU * blockDim.x) {
       C v[kU], w[kU];
 #pragma unroll
@@ -515,6 +525,7 @@ __global__ void __launch_bounds__(CShape<N1, N2, CS>::THREADS, 1) k_c2c_cluster_
     mbar_init(&arrived, 1);
     mbar_arrive_expect(&arrived, (unsigned)(S::WB * N2 * sizeof(C)) + (a.stall ? 16u : 0u));
   }
+  allow_dependents();
   cluster_arrive();
   const unsigned c = cluster_rank();
   const long long tr = blockIdx.x / CS;
@@ -531,11 +542,18 @@ __global__ void __launch_bounds__(CShape<N1, N2, CS>::THREADS, 1) k_c2c_cluster_
     const C* in = static_cast<const C*>(a.in) + tr * a.dist + (long long)c * S::WA;
     constexpr int STEPS = (S::E > NTAB ? S::E : NTAB), TRIPS = (STEPS + S::THREADS - 1) / S::THREADS;
     C v[TRIPS], w[TRIPS];
+    // The plan's tables first (no earlier kernel writes them), then the
+    // input once the kernels it depends on have completed.
+#pragma unroll
+    for (int u = 0; u < TRIPS; u++) {
+      const int b = u * S::THREADS + threadIdx.x;
+      if (b < NTAB) w[u] = b < TA ? ga[b] : b < TA + TB ? gb[b - TA] : gk[b - TA - TB];
+    }
+    wait_prerequisites();
 #pragma unroll
     for (int u = 0; u < TRIPS; u++) {
       const int b = u * S::THREADS + threadIdx.x;
       if (b < S::E) v[u] = in[(long long)(b / S::WA) * N2 + b % S::WA];
-      if (b < NTAB) w[u] = b < TA ? ga[b] : b < TA + TB ? gb[b - TA] : gk[b - TA - TB];
     }
 #pragma unroll
     for (int u = 0; u < TRIPS; u++) {
