@@ -100,7 +100,7 @@ struct PlanImpl {
   RaderCore rader;
   bool use_rader = false;
   // CFft1D batches of at most clus.max_batch transforms: one thread-block
-  // cluster per transform (the latency form; f64 by default).
+  // cluster per transform (the latency form).
   ClusterCore clus;
   PlanOpts opts;         // tuning knobs (chfft_plan_set_config)
   DevBuf work;           // four-step workspace

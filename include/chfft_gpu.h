@@ -234,9 +234,10 @@ typedef struct chfft_plan_info {
   /* CFft1D latency form: batches of at most cluster_max_batch transforms run
    * one transform per thread-block cluster of cluster_ctas CTAs (N =
    * cluster_n1 x cluster_n2 split over the cluster, exchange through
-   * distributed shared memory); 0 when the plan has none. f64 plans of
-   * 7-smooth lengths from 64 to 2^20 with such a split, f32 plans only with
-   * CHFFT_CLUSTER=8 or 16 at plan creation (CHFFT_CLUSTER=0 turns it off). */
+   * distributed shared memory); 0 when the plan has none. Plans of
+   * 7-smooth lengths from 64 to 2^20 with such a split that fits a CTA's
+   * shared memory (CHFFT_CLUSTER=0 at plan creation turns it off, 8 or 16
+   * forces the cluster size). */
   int cluster_ctas;
   size_t cluster_n1, cluster_n2, cluster_max_batch;
 } chfft_plan_info;

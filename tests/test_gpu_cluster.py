@@ -2,9 +2,9 @@
 through the C ABI.
 
 One transform per thread-block cluster of 8 or 16 CTAs, N = n1 x n2 split
-over the cluster, the exchange through distributed shared memory. f64
-plans take it by default for batches up to chfft_plan_info.cluster_max_batch;
-f32 plans only with CHFFT_CLUSTER=8 or 16 at plan creation. Checked against
+over the cluster, the exchange through distributed shared memory. Plans
+take it for batches up to chfft_plan_info.cluster_max_batch (CHFFT_CLUSTER=0
+at plan creation turns it off, 8 or 16 forces the cluster size). Checked against
 the oracle (f64 relative L2 <= 1e-12, f32 <= 5e-6) for every method kind,
 lengths one CTA holds and lengths beyond it, both cluster sizes, batches
 around the threshold, in-place device calls and a captured CUDA graph.
