@@ -4,13 +4,14 @@
 //
 // The host side groups the jobs by (kind, length, option), builds each
 // distinct length's tables once (FP64-generated, like every plan), decides
-// per length between a one-CTA task and a four-step task chain, and writes
-// the task queue: four-step levels first (column tiles; row tiles, which
-// for Bluestein also run the spectrum product and the inverse FFT's first
-// pass; the inverse's last pass; real-kind post tasks), then the one-CTA tasks by decreasing
-// cost. The queue and every table live in device memory; a launch only
-// passes the input / output base pointers, so it can be captured once and
-// replayed.
+// per length between a one-CTA task and a four-step task chain (column
+// tiles; row tiles, which for Bluestein also run the spectrum product and
+// the inverse FFT's first pass; the inverse's last pass; real-kind post
+// tasks), and writes the task queue: the chains' steps interleaved item by
+// item with a lag of a few waves between an item's steps, one-CTA tasks
+// (by decreasing cost) filling the gaps and following. The queue and every
+// table live in device memory; a launch only passes the input / output
+// base pointers, so it can be captured once and replayed.
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -22,6 +23,7 @@
 #include <vector>
 
 #include "../../include/chfft_gpu.h"
+#include "jit.hpp"
 #include "k_batch.cuh"
 #include "plan.hpp"
 
@@ -43,8 +45,10 @@ bool batch_fits(const StageList& st, int tpb) {
 // to kBatchTileMax whose tile fits one CTA. Wider tiles mean fewer tasks, so
 // less per-task overhead (ticket, descriptor, waits, signal) per element.
 int fs_width(const StageList& st) {
+  int cap = kBatchTileMax;
+  if (const char* e = std::getenv("CHFFT_BATCH_TILE_MAX")) cap = std::max(kBatchTile, std::min(kBatchTileMax, std::atoi(e)));
   int w = kBatchTile;
-  while (w * 2 <= kBatchTileMax && batch_fits(st, w * 2)) w *= 2;
+  while (w * 2 <= cap && batch_fits(st, w * 2)) w *= 2;
   return w;
 }
 
@@ -322,7 +326,13 @@ int chfft_batch_create(int dtype, const chfft_batch_job* jobs, size_t njobs, chf
     auto core_len = [](int kind, long long n) { return kind == BK_C2C ? n : kind == BK_MDCT ? n / 4 : n / 2; };
     std::vector<BatchItem> items(js.size());
     long long work_elems = 0;
-    std::vector<BatchTask> lv[4], post, small_tasks;
+    // Four-step tasks per item and step: A (columns), then B / BB (rows),
+    // then C (Bluestein's last rows) or POST (real kinds' split).
+    struct Group {
+      int item, step;
+      std::vector<BatchTask> t;
+    };
+    std::vector<std::vector<Group>> chains;
     std::vector<std::pair<double, BatchTask>> small_sorted;
     int nctr = 0;
     for (size_t i = 0; i < js.size(); i++) {
@@ -397,24 +407,27 @@ int chfft_batch_create(int dtype, const chfft_batch_job* jobs, size_t njobs, chf
         const int na = (hb.fs.n2 + wa - 1) / wa, nb = (hb.fs.n1 + wb - 1) / wb;
         const int c0 = nctr;
         nctr += 4;
-        for (int t = 0; t < na; t++) lv[0].push_back({BT_FS_A, (int)i, wa, hb.blue ? 1 : 0, t, -1, 0, c0});
+        std::vector<Group> chain(hb.blue || x.kind != BK_C2C ? 3 : 2);
+        for (int g = 0; g < (int)chain.size(); g++) chain[g] = Group{(int)i, g, {}};
+        for (int t = 0; t < na; t++) chain[0].t.push_back({BT_FS_A, (int)i, wa, hb.blue ? 1 : 0, t, -1, 0, c0});
         if (hb.blue) {
           // Forward rows + spectrum + the inverse's rows (FS_BB), then the
           // inverse's n1-long rows with the chirp-out (FS_C).
           const int wc = fs_width(hb.ca.d.st), nc = (hb.fs.n2 + wc - 1) / wc;
-          for (int t = 0; t < nb; t++) lv[1].push_back({BT_FS_BB, (int)i, wb, 0, t, c0, na, c0 + 1});
-          for (int t = 0; t < nc; t++) lv[2].push_back({BT_FS_C, (int)i, wc, 0, t, c0 + 1, nb, -1});
+          for (int t = 0; t < nb; t++) chain[1].t.push_back({BT_FS_BB, (int)i, wb, 0, t, c0, na, c0 + 1});
+          for (int t = 0; t < nc; t++) chain[2].t.push_back({BT_FS_C, (int)i, wc, 0, t, c0 + 1, nb, -1});
         } else {
           const int bmode = x.kind == BK_C2C ? 0 : 3;
           // A task whose counter nobody waits for (the last step of a C2C
           // item) skips the signal and its store fence.
           const int b_sig = x.kind != BK_C2C ? c0 + 1 : -1;
-          for (int t = 0; t < nb; t++) lv[1].push_back({BT_FS_B, (int)i, wb, bmode, t, c0, na, b_sig});
+          for (int t = 0; t < nb; t++) chain[1].t.push_back({BT_FS_B, (int)i, wb, bmode, t, c0, na, b_sig});
         }
         if (x.kind != BK_C2C) {
           const int pairs = (int)((x.n + 3) / 4);
-          for (int q = 0; q * kPostChunk < pairs; q++) post.push_back({BT_POST, (int)i, 1, 0, q, c0 + 1, nb, -1});
+          for (int q = 0; q * kPostChunk < pairs; q++) chain[2].t.push_back({BT_POST, (int)i, 1, 0, q, c0 + 1, nb, -1});
         }
+        chains.push_back(std::move(chain));
       }
     }
     // ---- one-CTA tasks: consecutive items of one (kind, length, option), up to tpb per task
@@ -440,10 +453,54 @@ int chfft_batch_create(int dtype, const chfft_batch_job* jobs, size_t njobs, chf
                      [](const std::pair<double, BatchTask>& a, const std::pair<double, BatchTask>& c) {
                        return a.first > c.first;
                      });
+    // Queue order. Each four-step item's steps follow one another with a
+    // lag of at least `lag` tickets (about two waves of resident CTAs), so a
+    // step's inputs are normally complete when its CTAs start, and the items
+    // in flight keep their intermediates in L2 (the level-by-level order
+    // sent every intermediate through DRAM). A step is queued only after
+    // every task it waits for, so a waited-for task is always held by a CTA
+    // that is already running. One-CTA tasks (longest first) fill the gaps
+    // where no step is due yet, and then follow.
     std::vector<BatchTask> tasks;
-    for (auto& l : lv) tasks.insert(tasks.end(), l.begin(), l.end());
-    tasks.insert(tasks.end(), post.begin(), post.end());
-    for (auto& p : small_sorted) tasks.push_back(p.second);
+    {
+      long long lag = 4LL * num_sms();
+      if (const char* e = std::getenv("CHFFT_BATCH_LAG")) lag = std::max(0LL, std::atoll(e));
+      const size_t nchain = chains.size();
+      std::vector<int> next_step(nchain, 0);
+      std::vector<size_t> step_end(nchain, 0);  // queue length after the item's last queued step
+      size_t started = 0, small_next = 0, done_chains = 0;
+      auto emit = [&](size_t c) {
+        Group& g = chains[c][next_step[c]];
+        tasks.insert(tasks.end(), g.t.begin(), g.t.end());
+        step_end[c] = tasks.size();
+        if (++next_step[c] == (int)chains[c].size()) done_chains++;
+      };
+      size_t oldest = 0;  // chains before it are done
+      while (done_chains < nchain) {
+        while (oldest < started && next_step[oldest] == (int)chains[oldest].size()) oldest++;
+        // a due later step of a started item (oldest first)
+        size_t due = nchain;
+        for (size_t c = oldest; c < started; c++)
+          if (next_step[c] < (int)chains[c].size() && tasks.size() >= step_end[c] + (size_t)lag) {
+            due = c;
+            break;
+          }
+        if (due < nchain) {
+          emit(due);
+        } else if (started < nchain) {
+          emit(started++);
+        } else if (small_next < small_sorted.size()) {
+          tasks.push_back(small_sorted[small_next++].second);
+        } else {
+          for (size_t c = oldest; c < started; c++)
+            if (next_step[c] < (int)chains[c].size()) {
+              emit(c);
+              break;
+            }
+        }
+      }
+      for (; small_next < small_sorted.size(); small_next++) tasks.push_back(small_sorted[small_next].second);
+    }
     // ---- shared memory per CTA: the largest tile
     size_t smem = 16;
     for (const BatchTask& t : tasks) {

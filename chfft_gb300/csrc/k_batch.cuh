@@ -21,8 +21,9 @@
 // pass works on the rows the forward FFT's last pass already holds.
 // Dependencies are device counters: a task waits (bounded spin, thread 0)
 // until its counter reaches the number of tiles of the step it consumes,
-// and signals its own counter when done. Tasks are queued level by level, so
-// a waited-for task is always held by a CTA that is already running.
+// and signals its own counter when done. A step is queued after every task
+// it waits for (CTAs take tickets in order), so a waited-for task is always
+// held by a CTA that is already running.
 // Workspace written by other CTAs is read with L1-bypassing loads.
 #pragma once
 

@@ -128,3 +128,58 @@ def test_rader_matches_dft(n):
     x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
     ref = np.fft.fft(x)
     assert np.linalg.norm(rader(x) - ref) / np.linalg.norm(ref) < 1e-12
+
+
+def batch_queue(chains, smalls, lag):
+    """The uneven batch's queue order (csrc/batch.cu): chains[c] lists the
+    task counts of an item's steps; a later step is queued once `lag`
+    tickets followed its previous step, items start in order, one-CTA tasks
+    fill the gaps and follow. Returns the queue as (chain, step, k) or
+    ('s', k) entries."""
+    out = []
+    nxt = [0] * len(chains)
+    end = [0] * len(chains)
+    started = small_next = done = 0
+
+    def emit(c):
+        nonlocal done
+        out.extend((c, nxt[c], k) for k in range(chains[c][nxt[c]]))
+        end[c] = len(out)
+        nxt[c] += 1
+        if nxt[c] == len(chains[c]):
+            done += 1
+
+    while done < len(chains):
+        due = next((c for c in range(started) if nxt[c] < len(chains[c]) and len(out) >= end[c] + lag), None)
+        if due is not None:
+            emit(due)
+        elif started < len(chains):
+            started += 1
+            emit(started - 1)
+        elif small_next < smalls:
+            out.append(("s", small_next))
+            small_next += 1
+        else:
+            emit(next(c for c in range(started) if nxt[c] < len(chains[c])))
+    out.extend(("s", k) for k in range(small_next, smalls))
+    return out
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+@pytest.mark.parametrize("lag", [0, 16, 600])
+def test_batch_queue_dependencies_precede(seed, lag):
+    """Every task of a step follows every task of the step it waits for (so
+    a waited-for task is held by a running CTA: deadlock-free), each task is
+    queued once, and where enough work exists the lag separates the steps."""
+    rng = np.random.default_rng(seed)
+    chains = [list(rng.integers(1, 40, size=rng.integers(2, 4))) for _ in range(rng.integers(1, 200))]
+    smalls = int(rng.integers(0, 500))
+    q = batch_queue(chains, smalls, lag)
+    assert len(q) == sum(map(sum, chains)) + smalls
+    assert len(set(q)) == len(q)
+    pos = {e: i for i, e in enumerate(q)}
+    for c, steps in enumerate(chains):
+        for s in range(1, len(steps)):
+            first = min(pos[(c, s, k)] for k in range(steps[s]))
+            last_prev = max(pos[(c, s - 1, k)] for k in range(steps[s - 1]))
+            assert first > last_prev

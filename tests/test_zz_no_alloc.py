@@ -72,3 +72,31 @@ def test_noalloc_rejects_oversized_and_small_plans():
     small = cg.CFft1D.with_len(1024, np.float32)  # single-CTA plan: needs no scratch
     rc = fn(small.handle, cg.METHODS["forward"], d.data_ptr(), d.data_ptr(), 1, 0)
     assert rc == cg.EINVAL
+
+
+def test_noalloc_captures_into_a_graph():
+    """After one warm-up call, the entry point runs inside a global-mode
+    stream capture (where a cudaMalloc would fail the capture) and the
+    replayed graph gives numpy's FP64 result."""
+    fn = _entry()
+    n, batch = 65536, 8
+    p = cg.CFft1D.with_len(n, np.float32)
+    rng = np.random.default_rng(7)
+    x = (rng.standard_normal((batch, n)) + 1j * rng.standard_normal((batch, n))).astype(np.complex64)
+    d_in = torch.from_numpy(x.view(np.float32)).cuda()
+    d_out = torch.empty_like(d_in)
+    rc = fn(p.handle, cg.METHODS["forward"], d_in.data_ptr(), d_out.data_ptr(), batch,
+            torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, cg.lib().chfft_last_error().decode()
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, capture_error_mode="global"):
+        rc = fn(p.handle, cg.METHODS["forward"], d_in.data_ptr(), d_out.data_ptr(), batch,
+                torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, cg.lib().chfft_last_error().decode()
+    d_out.zero_()
+    g.replay()
+    torch.cuda.synchronize()
+    assert rel(d_out.cpu().numpy().view(np.complex64), np.fft.fft(x.astype(np.complex128), axis=-1)) <= 5e-6
+    assert torch.cuda.mem_get_info()[0] >= free_before - (64 << 20)  # no workspace growth beyond the graph's own pool
