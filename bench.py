@@ -483,6 +483,10 @@ def run_uneven(args):
     d_out = torch.empty(b.out_bytes, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
     sptr = stream.cuda_stream
+    # Tile widths per class of four-step items, timed on this batch
+    # (chfft_batch_autotune), before the checked and timed launches.
+    tiles_default = list(b.info().class_tile)
+    tune_ms = b.autotune(d_in.data_ptr(), d_out.data_ptr(), sptr, reps=3) if not args.no_batch_tune else None
     run = lambda: b.execute(d_in.data_ptr(), d_out.data_ptr(), sptr, graph=True)  # noqa: E731
     run()
     b.wait(sptr)
@@ -538,7 +542,9 @@ def run_uneven(args):
                                "20% RFft1D, 10% DCT-II, 10% MDCT 2048 sine; one work-queue launch in a CUDA graph",
                    "subset": args.uneven_subset,
                    "l2": "flushed between timed steps", "tasks": info.tasks, "ctas": info.ctas,
-                   "four_step_lengths": info.four_step_lengths, "one_cta_lengths": info.one_cta_lengths},
+                   "four_step_lengths": info.four_step_lengths, "one_cta_lengths": info.one_cta_lengths,
+                   "class_tiles": {"default": tiles_default, "autotuned": list(info.class_tile),
+                                   "autotune_best_ms": tune_ms}},
         "hbm_gbs": round(nbytes / (ms * 1e-3) / 1e9, 1),
         "roofline": {"bound": "hbm", "kernel": "k_batch", "achieved": round(nbytes / (ms * 1e-3) / 1e9, 1),
                      "peak": 6767.1, "unit": "GB/s", "frac": round(nbytes / (ms * 1e-3) / 1e9 / 6767.1, 4),
@@ -1000,6 +1006,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch-tune", action="store_true",
+                    help="uneven workload: keep the default tile widths (skip chfft_batch_autotune)")
     ap.add_argument("--uneven-subset", default="all", choices=["all", "small", "big_c2c", "big_prime", "big_real"],
                     help="uneven workload: time one class of its jobs (profiling)")
     ap.add_argument("--small", action="store_true",

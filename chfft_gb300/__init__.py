@@ -482,7 +482,8 @@ class BatchJob(ctypes.Structure):
 class BatchInfo(ctypes.Structure):
     _fields_ = [("jobs", ctypes.c_size_t), ("tasks", ctypes.c_size_t), ("ctas", ctypes.c_uint),
                 ("smem_per_cta", ctypes.c_size_t), ("workspace_bytes", ctypes.c_size_t),
-                ("four_step_lengths", ctypes.c_size_t), ("one_cta_lengths", ctypes.c_size_t)]
+                ("four_step_lengths", ctypes.c_size_t), ("one_cta_lengths", ctypes.c_size_t),
+                ("class_tile", ctypes.c_int * 12)]
 
 
 KINDS = {"cfft1d": KIND_CFFT1D, "rfft1d": KIND_RFFT1D, "dct1d": KIND_DCT1D, "mdct1d": KIND_MDCT1D}
@@ -524,6 +525,8 @@ class Batch:
             "chfft_batch_execute_graph": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
             "chfft_batch_wait": [ctypes.c_void_p, ctypes.c_void_p],
             "chfft_batch_get_info": [ctypes.c_void_p, ctypes.POINTER(BatchInfo)],
+            "chfft_batch_autotune": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_float)],
             "chfft_batch_destroy": [ctypes.c_void_p],
         }.items():
             getattr(L, name).argtypes = args
@@ -551,6 +554,13 @@ class Batch:
 
     def wait(self, stream: int = 0):
         _check(lib().chfft_batch_wait(self._h, ctypes.c_void_p(stream)))
+
+    def autotune(self, d_in: int, d_out: int, stream: int = 0, reps: int = 3) -> float:
+        """Per-class tile widths timed on this batch (chfft_batch_autotune); the winner's ms."""
+        best = ctypes.c_float(0)
+        _check(lib().chfft_batch_autotune(self._h, ctypes.c_void_p(d_in), ctypes.c_void_p(d_out),
+                                          ctypes.c_void_p(stream), reps, ctypes.byref(best)))
+        return best.value
 
 
 # ---- index arithmetic (bit-exact with the reference's plan code) -----------

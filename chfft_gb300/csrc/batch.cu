@@ -35,6 +35,9 @@ cudaError_t launch_batch(const BatchArgs& a, unsigned blocks, size_t smem, cudaS
 namespace {
 
 constexpr size_t kBatchSmemCap = 100 * 1024;  // per CTA: two CTAs of 512 threads per SM
+// Tile classes of four-step items: kind group (C2C, C2C Bluestein, real
+// kinds) x four-step length (<= 2^14, <= 2^15, <= 2^16, larger).
+constexpr int kBatchClasses = 12;
 constexpr int kMaxSplit = 512;                // four-step factors in the batch kernel
 
 bool batch_fits(const StageList& st, int tpb) {
@@ -44,9 +47,7 @@ bool batch_fits(const StageList& st, int tpb) {
 // Four-step tile width of a core: the widest power of two from kBatchTile
 // to kBatchTileMax whose tile fits one CTA. Wider tiles mean fewer tasks, so
 // less per-task overhead (ticket, descriptor, waits, signal) per element.
-int fs_width(const StageList& st) {
-  int cap = kBatchTileMax;
-  if (const char* e = std::getenv("CHFFT_BATCH_TILE_MAX")) cap = std::max(kBatchTile, std::min(kBatchTileMax, std::atoi(e)));
+int fs_width(const StageList& st, int cap = kBatchTileMax) {
   int w = kBatchTile;
   while (w * 2 <= cap && batch_fits(st, w * 2)) w *= 2;
   return w;
@@ -201,10 +202,21 @@ struct KindTables {
 
 }  // namespace
 
+// A four-step item of the batch: its tables, its first counter and its
+// tile class (for the per-class tile caps).
+struct BigRef {
+  int item, big, c0, cls;
+};
+
 struct BatchImpl {
   std::vector<std::unique_ptr<HostCore>> smalls;
   std::vector<std::unique_ptr<HostBig>> bigs;
   std::vector<std::unique_ptr<KindTables>> kinds;
+  std::vector<BatchItem> items;                        // host copy (queue order of the jobs)
+  std::vector<BigRef> big_items;
+  std::vector<std::pair<double, BatchTask>> small_sorted;  // one-CTA tasks, longest first
+  int caps[kBatchClasses] = {};                        // widest tile per class
+  bool class_used[kBatchClasses] = {};
   DevBuf d_items, d_tasks, d_ctr, d_work;
   int ntasks = 0, nitems = 0, nctr = 0, nbig = 0;
   size_t smem = 0, work_bytes = 0;
@@ -218,10 +230,20 @@ struct BatchImpl {
   cudaStream_t g_stream = nullptr;
 
   ~BatchImpl() {
-    if (graph_exec) cudaGraphExecDestroy(graph_exec);
-    if (graph) cudaGraphDestroy(graph);
+    drop_graph();
     if (stream) cudaStreamDestroy(stream);
   }
+
+  void drop_graph() {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (graph) cudaGraphDestroy(graph);
+    graph_exec = nullptr;
+    graph = nullptr;
+  }
+
+  // The task queue for the current tile caps, uploaded (see the queue-order
+  // comment inside), and the shared memory per CTA it needs.
+  void build_tasks(cudaStream_t s);
 
   void enqueue(const void* d_in, void* d_out, cudaStream_t s) {
     CHFFT_CUDA(cudaMemsetAsync(d_ctr.p, 0, (size_t)(nctr + 2) * sizeof(int), s));
@@ -242,6 +264,112 @@ struct BatchImpl {
     CHFFT_CUDA(launch_batch(a, blocks, smem, s));
   }
 };
+
+void BatchImpl::build_tasks(cudaStream_t s) {
+  // Four-step tasks per item and step: A (columns), then B / BB (rows),
+  // then C (Bluestein's last rows) or POST (real kinds' split).
+  struct Group {
+    int item, step;
+    std::vector<BatchTask> t;
+  };
+  std::vector<std::vector<Group>> chains;
+  for (const BigRef& r : big_items) {
+    const int i = r.item, c0 = r.c0;
+    const BatchItem& it = items[i];
+    const HostBig& hb = *bigs[r.big];
+    const int cap = caps[r.cls];
+    const int wa = fs_width(hb.ca.d.st, cap), wb = fs_width(hb.cb.d.st, cap);
+    const int na = (hb.fs.n2 + wa - 1) / wa, nb = (hb.fs.n1 + wb - 1) / wb;
+    std::vector<Group> chain(hb.blue || it.kind != BK_C2C ? 3 : 2);
+    for (int g = 0; g < (int)chain.size(); g++) chain[g] = Group{i, g, {}};
+    for (int t = 0; t < na; t++) chain[0].t.push_back({BT_FS_A, i, wa, hb.blue ? 1 : 0, t, -1, 0, c0});
+    if (hb.blue) {
+      // Forward rows + spectrum + the inverse's rows (FS_BB), then the
+      // inverse's n1-long rows with the chirp-out (FS_C).
+      const int wc = fs_width(hb.ca.d.st, cap), nc = (hb.fs.n2 + wc - 1) / wc;
+      for (int t = 0; t < nb; t++) chain[1].t.push_back({BT_FS_BB, i, wb, 0, t, c0, na, c0 + 1});
+      for (int t = 0; t < nc; t++) chain[2].t.push_back({BT_FS_C, i, wc, 0, t, c0 + 1, nb, -1});
+    } else {
+      const int bmode = it.kind == BK_C2C ? 0 : 3;
+      // A task whose counter nobody waits for (the last step of a C2C
+      // item) skips the signal and its store fence.
+      const int b_sig = it.kind != BK_C2C ? c0 + 1 : -1;
+      for (int t = 0; t < nb; t++) chain[1].t.push_back({BT_FS_B, i, wb, bmode, t, c0, na, b_sig});
+    }
+    if (it.kind != BK_C2C) {
+      const int pairs = (it.n + 3) / 4;
+      for (int q = 0; q * kPostChunk < pairs; q++) chain[2].t.push_back({BT_POST, i, 1, 0, q, c0 + 1, nb, -1});
+    }
+    chains.push_back(std::move(chain));
+  }
+  // Queue order. Each four-step item's steps follow one another with a
+  // lag of at least `lag` tickets (about two waves of resident CTAs), so a
+  // step's inputs are normally complete when its CTAs start, and the items
+  // in flight keep their intermediates in L2 (the level-by-level order
+  // sent every intermediate through DRAM). A step is queued only after
+  // every task it waits for, so a waited-for task is always held by a CTA
+  // that is already running. One-CTA tasks (longest first) fill the gaps
+  // where no step is due yet, and then follow.
+  std::vector<BatchTask> tasks;
+  {
+    long long lag = 4LL * num_sms();
+    if (const char* e = std::getenv("CHFFT_BATCH_LAG")) lag = std::max(0LL, std::atoll(e));
+    const size_t nchain = chains.size();
+    std::vector<int> next_step(nchain, 0);
+    std::vector<size_t> step_end(nchain, 0);  // queue length after the item's last queued step
+    size_t started = 0, small_next = 0, done_chains = 0;
+    auto emit = [&](size_t c) {
+      Group& g = chains[c][next_step[c]];
+      tasks.insert(tasks.end(), g.t.begin(), g.t.end());
+      step_end[c] = tasks.size();
+      if (++next_step[c] == (int)chains[c].size()) done_chains++;
+    };
+    size_t oldest = 0;  // chains before it are done
+    while (done_chains < nchain) {
+      while (oldest < started && next_step[oldest] == (int)chains[oldest].size()) oldest++;
+      // a due later step of a started item (oldest first)
+      size_t due = nchain;
+      for (size_t c = oldest; c < started; c++)
+        if (next_step[c] < (int)chains[c].size() && tasks.size() >= step_end[c] + (size_t)lag) {
+          due = c;
+          break;
+        }
+      if (due < nchain) {
+        emit(due);
+      } else if (started < nchain) {
+        emit(started++);
+      } else if (small_next < small_sorted.size()) {
+        tasks.push_back(small_sorted[small_next++].second);
+      } else {
+        for (size_t c = oldest; c < started; c++)
+          if (next_step[c] < (int)chains[c].size()) {
+            emit(c);
+            break;
+          }
+      }
+    }
+    for (; small_next < small_sorted.size(); small_next++) tasks.push_back(small_sorted[small_next].second);
+  }
+  // ---- shared memory per CTA: the largest tile
+  size_t smem_need = 16;
+  for (const BatchTask& t : tasks) {
+    const BatchItem& it = items[t.item];
+    size_t need = 0;
+    if (t.type == BT_SMALL) need = (size_t)t.count * smem_ld(it.core.st.n) * 8;
+    else if (t.type == BT_FS_A || t.type == BT_FS_C) need = (size_t)t.count * smem_ld(it.ca.st.n) * 8;
+    else if (t.type == BT_FS_B || t.type == BT_FS_BB) need = (size_t)t.count * smem_ld(it.cb.st.n) * 8;
+    smem_need = std::max(smem_need, need);
+  }
+  // ---- upload
+  ntasks = (int)tasks.size();
+  smem = smem_need;
+  d_tasks.ensure(std::max<size_t>(1, tasks.size()) * sizeof(BatchTask));
+  if (!tasks.empty())
+    CHFFT_CUDA(cudaMemcpyAsync(d_tasks.p, tasks.data(), tasks.size() * sizeof(BatchTask), cudaMemcpyHostToDevice, s));
+  blocks = (unsigned)std::max(1, ntasks);
+  CHFFT_CUDA(cudaStreamSynchronize(s));
+  drop_graph();  // a captured launch holds the old task count
+}
 
 }  // namespace chfft
 
@@ -326,14 +454,8 @@ int chfft_batch_create(int dtype, const chfft_batch_job* jobs, size_t njobs, chf
     auto core_len = [](int kind, long long n) { return kind == BK_C2C ? n : kind == BK_MDCT ? n / 4 : n / 2; };
     std::vector<BatchItem> items(js.size());
     long long work_elems = 0;
-    // Four-step tasks per item and step: A (columns), then B / BB (rows),
-    // then C (Bluestein's last rows) or POST (real kinds' split).
-    struct Group {
-      int item, step;
-      std::vector<BatchTask> t;
-    };
-    std::vector<std::vector<Group>> chains;
-    std::vector<std::pair<double, BatchTask>> small_sorted;
+
+    std::vector<std::pair<double, BatchTask>>& small_sorted = B.small_sorted;
     int nctr = 0;
     for (size_t i = 0; i < js.size(); i++) {
       const Job& x = js[i];
@@ -402,32 +524,12 @@ int chfft_batch_create(int dtype, const chfft_batch_job* jobs, size_t njobs, chf
           it.work2_off = work_elems * 8;
           work_elems += hb.m;
         }
-        // tasks of this item
-        const int wa = fs_width(hb.ca.d.st), wb = fs_width(hb.cb.d.st);
-        const int na = (hb.fs.n2 + wa - 1) / wa, nb = (hb.fs.n1 + wb - 1) / wb;
-        const int c0 = nctr;
+        // its tasks come from build_tasks (tile widths per class)
+        const int grp = hb.blue ? 1 : (x.kind != BK_C2C ? 2 : 0);
+        const int bucket = hb.m <= (1 << 14) ? 0 : hb.m <= (1 << 15) ? 1 : hb.m <= (1 << 16) ? 2 : 3;
+        B.big_items.push_back(BigRef{(int)i, big_of[nc], nctr, grp * 4 + bucket});
+        B.class_used[grp * 4 + bucket] = true;
         nctr += 4;
-        std::vector<Group> chain(hb.blue || x.kind != BK_C2C ? 3 : 2);
-        for (int g = 0; g < (int)chain.size(); g++) chain[g] = Group{(int)i, g, {}};
-        for (int t = 0; t < na; t++) chain[0].t.push_back({BT_FS_A, (int)i, wa, hb.blue ? 1 : 0, t, -1, 0, c0});
-        if (hb.blue) {
-          // Forward rows + spectrum + the inverse's rows (FS_BB), then the
-          // inverse's n1-long rows with the chirp-out (FS_C).
-          const int wc = fs_width(hb.ca.d.st), nc = (hb.fs.n2 + wc - 1) / wc;
-          for (int t = 0; t < nb; t++) chain[1].t.push_back({BT_FS_BB, (int)i, wb, 0, t, c0, na, c0 + 1});
-          for (int t = 0; t < nc; t++) chain[2].t.push_back({BT_FS_C, (int)i, wc, 0, t, c0 + 1, nb, -1});
-        } else {
-          const int bmode = x.kind == BK_C2C ? 0 : 3;
-          // A task whose counter nobody waits for (the last step of a C2C
-          // item) skips the signal and its store fence.
-          const int b_sig = x.kind != BK_C2C ? c0 + 1 : -1;
-          for (int t = 0; t < nb; t++) chain[1].t.push_back({BT_FS_B, (int)i, wb, bmode, t, c0, na, b_sig});
-        }
-        if (x.kind != BK_C2C) {
-          const int pairs = (int)((x.n + 3) / 4);
-          for (int q = 0; q * kPostChunk < pairs; q++) chain[2].t.push_back({BT_POST, (int)i, 1, 0, q, c0 + 1, nb, -1});
-        }
-        chains.push_back(std::move(chain));
       }
     }
     // ---- one-CTA tasks: consecutive items of one (kind, length, option), up to tpb per task
@@ -453,80 +555,18 @@ int chfft_batch_create(int dtype, const chfft_batch_job* jobs, size_t njobs, chf
                      [](const std::pair<double, BatchTask>& a, const std::pair<double, BatchTask>& c) {
                        return a.first > c.first;
                      });
-    // Queue order. Each four-step item's steps follow one another with a
-    // lag of at least `lag` tickets (about two waves of resident CTAs), so a
-    // step's inputs are normally complete when its CTAs start, and the items
-    // in flight keep their intermediates in L2 (the level-by-level order
-    // sent every intermediate through DRAM). A step is queued only after
-    // every task it waits for, so a waited-for task is always held by a CTA
-    // that is already running. One-CTA tasks (longest first) fill the gaps
-    // where no step is due yet, and then follow.
-    std::vector<BatchTask> tasks;
-    {
-      long long lag = 4LL * num_sms();
-      if (const char* e = std::getenv("CHFFT_BATCH_LAG")) lag = std::max(0LL, std::atoll(e));
-      const size_t nchain = chains.size();
-      std::vector<int> next_step(nchain, 0);
-      std::vector<size_t> step_end(nchain, 0);  // queue length after the item's last queued step
-      size_t started = 0, small_next = 0, done_chains = 0;
-      auto emit = [&](size_t c) {
-        Group& g = chains[c][next_step[c]];
-        tasks.insert(tasks.end(), g.t.begin(), g.t.end());
-        step_end[c] = tasks.size();
-        if (++next_step[c] == (int)chains[c].size()) done_chains++;
-      };
-      size_t oldest = 0;  // chains before it are done
-      while (done_chains < nchain) {
-        while (oldest < started && next_step[oldest] == (int)chains[oldest].size()) oldest++;
-        // a due later step of a started item (oldest first)
-        size_t due = nchain;
-        for (size_t c = oldest; c < started; c++)
-          if (next_step[c] < (int)chains[c].size() && tasks.size() >= step_end[c] + (size_t)lag) {
-            due = c;
-            break;
-          }
-        if (due < nchain) {
-          emit(due);
-        } else if (started < nchain) {
-          emit(started++);
-        } else if (small_next < small_sorted.size()) {
-          tasks.push_back(small_sorted[small_next++].second);
-        } else {
-          for (size_t c = oldest; c < started; c++)
-            if (next_step[c] < (int)chains[c].size()) {
-              emit(c);
-              break;
-            }
-        }
-      }
-      for (; small_next < small_sorted.size(); small_next++) tasks.push_back(small_sorted[small_next].second);
-    }
-    // ---- shared memory per CTA: the largest tile
-    size_t smem = 16;
-    for (const BatchTask& t : tasks) {
-      const BatchItem& it = items[t.item];
-      size_t need = 0;
-      if (t.type == BT_SMALL) need = (size_t)t.count * smem_ld(it.core.st.n) * 8;
-      else if (t.type == BT_FS_A || t.type == BT_FS_C) need = (size_t)t.count * smem_ld(it.ca.st.n) * 8;
-      else if (t.type == BT_FS_B || t.type == BT_FS_BB) need = (size_t)t.count * smem_ld(it.cb.st.n) * 8;
-      smem = std::max(smem, need);
-    }
     // ---- upload
     B.nitems = (int)items.size();
-    B.ntasks = (int)tasks.size();
     B.nctr = nctr;
-    B.smem = smem;
     B.d_items.ensure(std::max<size_t>(1, items.size()) * sizeof(BatchItem));
-    B.d_tasks.ensure(std::max<size_t>(1, tasks.size()) * sizeof(BatchTask));
     B.d_ctr.ensure((size_t)(nctr + 2) * sizeof(int));
     B.work_bytes = (size_t)work_elems * 8;
     B.d_work.ensure(std::max<size_t>(B.work_bytes, 256));
     if (!items.empty())
       CHFFT_CUDA(cudaMemcpyAsync(B.d_items.p, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice, s));
-    if (!tasks.empty())
-      CHFFT_CUDA(cudaMemcpyAsync(B.d_tasks.p, tasks.data(), tasks.size() * sizeof(BatchTask), cudaMemcpyHostToDevice, s));
-    B.blocks = (unsigned)std::max(1, B.ntasks);
-    CHFFT_CUDA(cudaStreamSynchronize(s));
+    B.items = std::move(items);
+    for (int& c : B.caps) c = kBatchTileMax;
+    B.build_tasks(s);
   } catch (const Fail& f) {
     return record_error(f.code, f.msg);
   }
@@ -581,6 +621,62 @@ int chfft_batch_wait(chfft_batch batch, void* stream) {
   return CHFFT_OK;
 }
 
+int chfft_batch_autotune(chfft_batch batch, const void* d_in, void* d_out, void* stream, int reps, float* best_ms) {
+  using namespace chfft;
+  if (!batch || reps < 1) return record_error(CHFFT_EINVAL, "null batch or reps < 1");
+  BatchImpl& B = batch->impl;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  try {
+    CHFFT_CUDA(cudaEventCreate(&e0));
+    CHFFT_CUDA(cudaEventCreate(&e1));
+    int err = 0;
+    // Median of `reps` launches of the current task list (one launch first).
+    auto time_it = [&]() -> float {
+      B.build_tasks(B.stream);
+      B.enqueue(d_in, d_out, s);
+      std::vector<float> v;
+      for (int r = 0; r < reps; r++) {
+        CHFFT_CUDA(cudaEventRecord(e0, s));
+        B.enqueue(d_in, d_out, s);
+        CHFFT_CUDA(cudaEventRecord(e1, s));
+        CHFFT_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        CHFFT_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        v.push_back(ms);
+      }
+      CHFFT_CUDA(cudaMemcpy(&err, static_cast<int*>(B.d_ctr.p) + B.nctr + 1, sizeof(int), cudaMemcpyDeviceToHost));
+      if (err) throw Fail{CHFFT_ETIMEOUT, "a batch task waited too long for its dependencies"};
+      std::sort(v.begin(), v.end());
+      return v[v.size() / 2];
+    };
+    float best = time_it();
+    for (int c = 0; c < kBatchClasses; c++) {
+      if (!B.class_used[c]) continue;
+      int keep = B.caps[c];
+      for (int cap : {16, 32, 64}) {
+        if (cap == keep) continue;
+        B.caps[c] = cap;
+        const float t = time_it();
+        if (t < best) {
+          best = t;
+          keep = cap;
+        }
+      }
+      B.caps[c] = keep;
+    }
+    B.build_tasks(B.stream);
+    if (best_ms) *best_ms = best;
+  } catch (const Fail& f) {
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    return record_error(f.code, f.msg);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return CHFFT_OK;
+}
+
 int chfft_batch_get_info(chfft_batch batch, chfft_batch_info* info) {
   if (!batch || !info) return chfft::record_error(CHFFT_EINVAL, "null argument");
   const chfft::BatchImpl& B = batch->impl;
@@ -592,6 +688,7 @@ int chfft_batch_get_info(chfft_batch batch, chfft_batch_info* info) {
   info->workspace_bytes = B.work_bytes;
   info->four_step_lengths = B.bigs.size();
   info->one_cta_lengths = B.smalls.size();
+  for (int c = 0; c < chfft::kBatchClasses && c < 12; c++) info->class_tile[c] = B.class_used[c] ? B.caps[c] : 0;
   return CHFFT_OK;
 }
 

@@ -199,6 +199,12 @@ typedef struct chfft_batch_info {
   size_t smem_per_cta;
   size_t workspace_bytes;     /* four-step intermediates */
   size_t four_step_lengths, one_cta_lengths;
+  /* Widest four-step tile (columns / rows) per class of four-step items,
+   * 0 for a class the batch has: index group * 4 + size, group 0 C2C,
+   * 1 C2C Bluestein, 2 real kinds; size 0..3 for a four-step length of at
+   * most 2^14, 2^15, 2^16, or more. Default 64 (the widest that fits a
+   * CTA); chfft_batch_autotune times the alternatives. */
+  int class_tile[12];
 } chfft_batch_info;
 
 /* Builds every table and the task queue (device memory). */
@@ -213,6 +219,16 @@ CHFFT_API int chfft_batch_execute_graph(chfft_batch batch, const void* d_in, voi
  * dependencies (the launch then returned without hanging). */
 CHFFT_API int chfft_batch_wait(chfft_batch batch, void* stream);
 CHFFT_API int chfft_batch_get_info(chfft_batch batch, chfft_batch_info* info);
+/* Tile widths chosen by timing this batch (no counterpart in the reference,
+ * whose factor order is fixed, src/prime_factorization.rs:66-113): for each
+ * class of four-step items present, in turn, the widest tile is tried at 16,
+ * 32 and 64 with the other classes held, each candidate timed as the median
+ * of `reps` launches on d_in / d_out (CUDA events on `stream`), and the class
+ * keeps the fastest. The batch then runs with the chosen widths; *best_ms
+ * (may be null) gets the winner's time. CHFFT_ETIMEOUT if a launch's
+ * dependency wait gave up. */
+CHFFT_API int chfft_batch_autotune(chfft_batch batch, const void* d_in, void* d_out, void* stream, int reps,
+                                   float* best_ms);
 CHFFT_API int chfft_batch_destroy(chfft_batch batch);
 
 /* ---- plan inspection ---------------------------------------------------- */

@@ -162,3 +162,33 @@ def test_batch_bounded_wait_runs_out_and_recovers(monkeypatch):
     host_out = d_out.cpu().numpy()
     for (kind, n, method, option), (_, oo), x in zip(specs, b.offsets, xs):
         assert rel(out_view(kind, n, host_out[oo:]), expected(kind, n, method, option, x)) <= 5e-6
+
+
+def test_batch_autotune_picks_class_tiles_and_stays_correct():
+    """chfft_batch_autotune times tile widths 16 / 32 / 64 per class of
+    four-step items on the batch itself; afterwards every used class has a
+    width from that set, unused classes report 0, and every job still
+    matches the oracle (normal launch and graph replay)."""
+    specs = [("cfft1d", n, "forward", 0) for n in (16384, 20000, 40000, 65536, 10007, 65521)] * 3
+    specs += [("rfft1d", n, "forward", 0) for n in (40000, 65536)] * 2
+    specs += [("cfft1d", 1000, "forward", 0)] * 20
+    b = cg.Batch(specs)
+    before = list(b.info().class_tile)
+    assert all(t in (0, 64) for t in before) and any(before)
+    host_in, xs = make_inputs(specs, b)
+    d_in = torch.from_numpy(host_in).cuda()
+    d_out = torch.zeros(max(b.out_bytes, 16), dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    ms = b.autotune(d_in.data_ptr(), d_out.data_ptr(), stream, reps=3)
+    assert ms > 0
+    after = list(b.info().class_tile)
+    for t0, t1 in zip(before, after):
+        assert (t0 == 0) == (t1 == 0)
+        assert t1 in (0, 16, 32, 64)
+    for graph in (False, True):
+        d_out.zero_()
+        b.execute(d_in.data_ptr(), d_out.data_ptr(), stream, graph=graph)
+        b.wait(stream)
+        host_out = d_out.cpu().numpy()
+        for (kind, n, method, option), (_, oo), x in zip(specs, b.offsets, xs):
+            assert rel(out_view(kind, n, host_out[oo:]), expected(kind, n, method, option, x)) <= 5e-6
