@@ -40,7 +40,7 @@ METHODS = {
 }
 _BACKWARD = {"backward", "backward0", "backwardu", "backwardn", "backward0i", "backwardui"}
 
-KIND_CFFT1D, KIND_CFFT2D, KIND_RFFT1D, KIND_DCT1D, KIND_MDCT1D = range(5)
+KIND_CFFT1D, KIND_CFFT2D, KIND_RFFT1D, KIND_DCT1D, KIND_MDCT1D, KIND_CFFT3D = range(6)
 
 
 class ChfftError(RuntimeError):
@@ -62,7 +62,7 @@ class PlanInfo(ctypes.Structure):
         ("seq_per_cta", ctypes.c_int), ("threads_per_cta", ctypes.c_int), ("smem_per_cta", ctypes.c_size_t),
         ("in_elems", ctypes.c_size_t), ("out_elems", ctypes.c_size_t), ("device_bytes", ctypes.c_size_t),
         ("cluster_ctas", ctypes.c_int), ("cluster_n1", ctypes.c_size_t), ("cluster_n2", ctypes.c_size_t),
-        ("cluster_max_batch", ctypes.c_size_t),
+        ("cluster_max_batch", ctypes.c_size_t), ("len_l", ctypes.c_size_t),
     ]
 
 
@@ -81,6 +81,7 @@ def lib() -> ctypes.CDLL:
     sigs = {
         "chfft_cfft1d_create": [i, sz, pp],
         "chfft_cfft2d_create": [i, sz, sz, pp],
+        "chfft_cfft3d_create": [i, sz, sz, sz, pp],
         "chfft_rfft1d_create": [i, sz, pp],
         "chfft_dct1d_create": [i, i, sz, i, pp],
         "chfft_mdct1d_create": [i, sz, i, vp, pp],
@@ -90,6 +91,7 @@ def lib() -> ctypes.CDLL:
         "chfft_dct1d_setup": [vp, i, sz, i],
         "chfft_execute": [vp, i, vp, sz, vp, sz],
         "chfft_execute_2d": [vp, i, vp, sz, sz, vp],
+        "chfft_execute_3d": [vp, i, vp, sz, sz, sz, vp],
         "chfft_execute_batch": [vp, i, vp, vp, sz],
         "chfft_execute_device": [vp, i, vp, vp, sz, vp],
         "chfft_plan_wait": [vp, vp],
@@ -316,6 +318,50 @@ class CFft2D(_Plan):
         out = np.empty((m, n), _cplx(self._did))
         _check(lib().chfft_execute_2d(self._h, METHODS[method], _ptr(source), m, n, _ptr(out)))
         self._shape = (m, n)
+        return out
+
+    def forward(self, source): return self._run("forward", source)
+    def forward0(self, source): return self._run("forward0", source)
+    def forwardu(self, source): return self._run("forwardu", source)
+    def forwardn(self, source): return self._run("forwardn", source)
+    def backward(self, source): return self._run("backward", source)
+    def backward0(self, source): return self._run("backward0", source)
+    def backwardu(self, source): return self._run("backwardu", source)
+
+
+class CFft3D(_Plan):
+    """3-D complex transform of (len_l, len_m, len_n) row-major arrays: no
+    reference counterpart (chfft stops at CFft2D); CFft2D's methods and
+    scales extended by one axis."""
+
+    kind = KIND_CFFT3D
+
+    def __init__(self, len_l: int = 0, len_m: int = 0, len_n: int = 0, dtype=np.float64):
+        super().__init__(dtype)
+        self._shape = (len_l, len_m, len_n)
+        _check(lib().chfft_cfft3d_create(self._did, len_l, len_m, len_n, ctypes.byref(self._h)))
+
+    @classmethod
+    def with_len(cls, len_l: int, len_m: int, len_n: int, dtype=np.float64):
+        return cls(len_l, len_m, len_n, dtype)
+
+    def _in_dtype(self, method):
+        return _cplx(self._did)
+
+    _out_dtype = _in_dtype
+
+    def _sizes(self, back):
+        n = self._shape[0] * self._shape[1] * self._shape[2]
+        return n, n
+
+    def _run(self, method, source):
+        source = np.ascontiguousarray(source, _cplx(self._did))
+        if source.size == 0:
+            return np.empty(source.shape, _cplx(self._did))
+        l, m, n = source.shape
+        out = np.empty((l, m, n), _cplx(self._did))
+        _check(lib().chfft_execute_3d(self._h, METHODS[method], _ptr(source), l, m, n, _ptr(out)))
+        self._shape = (l, m, n)
         return out
 
     def forward(self, source): return self._run("forward", source)
@@ -601,7 +647,7 @@ def chirp_index_device(len: int, d_out: int, stream: int = 0):
 
 
 __all__ = [
-    "CFft1D", "CFft2D", "RFft1D", "Dct1D", "DctType", "Mdct1D", "sine_window", "vorbis_window",
+    "CFft1D", "CFft2D", "CFft3D", "RFft1D", "Dct1D", "DctType", "Mdct1D", "sine_window", "vorbis_window",
     "ChfftError", "InvalidLength", "PlanInfo", "factorize", "digit_reversal", "swap_list", "chirp_index_device",
     "lib", "version",
 ]

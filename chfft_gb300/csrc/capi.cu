@@ -74,6 +74,20 @@ int chfft_cfft2d_create(int dtype, size_t len_m, size_t len_n, chfft_plan* out) 
   });
 }
 
+int chfft_cfft3d_create(int dtype, size_t len_l, size_t len_m, size_t len_n, chfft_plan* out) {
+  if (!valid_dtype(dtype)) return chfft::set_error(CHFFT_EINVAL, "unknown dtype");
+  if (len_l > (1u << 31) || len_m > (1u << 31) || len_n > (1u << 31)) return chfft::set_error(CHFFT_EINVAL_LEN, "invalid length");
+  return create(out, [&](PlanImpl& p) -> int {
+    p.kind = CHFFT_KIND_CFFT3D;
+    p.dtype = dtype;
+    p.len_l = (long long)len_l;
+    p.len_m = (long long)len_m;
+    p.len_n = (long long)len_n;
+    p.len = p.len_l * p.len_m * p.len_n;
+    return CHFFT_OK;
+  });
+}
+
 int chfft_rfft1d_create(int dtype, size_t len, chfft_plan* out) {
   if (!valid_dtype(dtype)) return chfft::set_error(CHFFT_EINVAL, "unknown dtype");
   if ((len & 1) || len == 0) return chfft::set_error(CHFFT_EINVAL_LEN, "invalid length");
@@ -174,6 +188,7 @@ int chfft_execute(chfft_plan plan, int method, const void* src, size_t src_len, 
   if (!plan) return chfft::set_error(CHFFT_EINVAL, "null plan");
   PlanImpl& p = plan->impl;
   if (p.kind == CHFFT_KIND_CFFT2D) return chfft::set_error(CHFFT_EINVAL, "use chfft_execute_2d for CFft2D");
+  if (p.kind == CHFFT_KIND_CFFT3D) return chfft::set_error(CHFFT_EINVAL, "use chfft_execute_3d for CFft3D");
   chfft::MethodSpec ms = chfft::method_spec(p.kind, method);
   if (!ms.ok) return chfft::set_error(CHFFT_EINVAL, "method not offered by this type");
   return guarded([&]() -> int {
@@ -190,6 +205,28 @@ int chfft_execute(chfft_plan plan, int method, const void* src, size_t src_len, 
     if ((src_len && !src) || (dst_len && !dst)) return chfft::set_error(CHFFT_EINVAL, "null buffer");
     p.exec_host(ms, src, dst, 1);
     return CHFFT_OK;
+  });
+}
+
+int chfft_execute_3d(chfft_plan plan, int method, const void* src, size_t len_l, size_t len_m, size_t len_n,
+                     void* dst) {
+  if (!plan || plan->impl.kind != CHFFT_KIND_CFFT3D) return chfft::set_error(CHFFT_EINVAL, "not a CFft3D plan");
+  PlanImpl& p = plan->impl;
+  chfft::MethodSpec ms = chfft::method_spec(p.kind, method);
+  if (!ms.ok) return chfft::set_error(CHFFT_EINVAL, "method not offered by CFft3D");
+  return guarded([&]() -> int {
+    if (len_l == 0 || len_m == 0 || len_n == 0) return (int)CHFFT_OK;  // empty in, empty out (as CFft2D)
+    if ((long long)len_l != p.len_l || (long long)len_m != p.len_m || (long long)len_n != p.len_n) {
+      p.len_l = (long long)len_l;
+      p.len_m = (long long)len_m;
+      p.len_n = (long long)len_n;
+      p.len = p.len_l * p.len_m * p.len_n;
+      int rc = p.build();
+      if (rc != CHFFT_OK) return rc;
+    }
+    if (!src || !dst) return chfft::set_error(CHFFT_EINVAL, "null buffer");
+    p.exec_host(ms, src, dst, 1);
+    return (int)CHFFT_OK;
   });
 }
 
@@ -255,6 +292,7 @@ int chfft_plan_get_info(chfft_plan plan, chfft_plan_info* info) {
   info->dtype = p.dtype;
   info->len = (size_t)p.len;
   info->len_m = (size_t)p.len_m;
+  info->len_l = (size_t)p.len_l;
   info->len_n = (size_t)p.len_n;
   info->fft_len = (size_t)(p.use_big ? p.big.n : p.use_rader ? p.rader.n : p.core.n);
   info->algorithm = p.use_big ? (p.big.blue ? 3 : 2) : p.use_rader ? 4 : (p.core.blue ? 1 : 0);
@@ -282,7 +320,7 @@ int chfft_plan_get_info(chfft_plan plan, chfft_plan_info* info) {
   }
   info->in_elems = p.in_elems(false);
   info->out_elems = p.out_elems(false);
-  info->device_bytes = p.core.device_bytes() + p.core2.device_bytes() + p.big.device_bytes() + p.work.bytes +
+  info->device_bytes = p.core.device_bytes() + p.core2.device_bytes() + p.core3.device_bytes() + p.big.device_bytes() + p.work.bytes +
                        p.aux0.bytes + p.aux1.bytes + p.rader.device_bytes() + p.clus.device_bytes();
   info->cluster_ctas = p.clus.n ? p.clus.csize : 0;
   info->cluster_n1 = p.clus.n ? (size_t)p.clus.n1 : 0;

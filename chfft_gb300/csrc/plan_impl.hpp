@@ -43,6 +43,7 @@ inline MethodSpec method_spec(int kind, int m) {
   switch (kind) {
     case CHFFT_KIND_CFFT1D:
     case CHFFT_KIND_CFFT2D:
+    case CHFFT_KIND_CFFT3D:
     case CHFFT_KIND_RFFT1D:
       switch (m) {
         case CHFFT_FORWARD: case CHFFT_FORWARD0: set(false, S_ONE); break;
@@ -51,7 +52,7 @@ inline MethodSpec method_spec(int kind, int m) {
         case CHFFT_BACKWARD: set(true, S_N); break;
         case CHFFT_BACKWARD0: set(true, S_ONE); break;
         case CHFFT_BACKWARDU: set(true, S_UNITARY); break;
-        case CHFFT_BACKWARDN: if (kind != CHFFT_KIND_CFFT2D) set(true, S_N); break;
+        case CHFFT_BACKWARDN: if (kind != CHFFT_KIND_CFFT2D && kind != CHFFT_KIND_CFFT3D) set(true, S_N); break;
         case CHFFT_FORWARD0I: if (kind == CHFFT_KIND_CFFT1D) set(false, S_ONE); break;
         case CHFFT_BACKWARD0I: if (kind == CHFFT_KIND_CFFT1D) set(true, S_ONE); break;
         case CHFFT_FORWARDUI: if (kind == CHFFT_KIND_CFFT1D) set(false, S_UNITARY); break;
@@ -83,13 +84,14 @@ inline MethodSpec method_spec(int kind, int m) {
 
 struct PlanImpl {
   int kind = 0, dtype = 0;
-  long long len = 0, len_m = 0, len_n = 0;
+  long long len = 0, len_m = 0, len_n = 0, len_l = 0;
   int dct_type = CHFFT_DCT_TWO;
   bool ortho = false;
   int window = CHFFT_WINDOW_SINE;
   std::vector<unsigned char> custom_window;
   Core core;   // complex core (CFft1D: N; CFft2D rows: N; RFft1D/Dct1D: N/2; Mdct1D: N/4)
-  Core core2;  // CFft2D columns: M
+  Core core2;  // CFft2D / CFft3D columns: M
+  Core core3;  // CFft3D outer axis: L
   BigCore big;           // CFft1D beyond one CTA (four-step)
   bool use_big = false;
   // CFft1D of a prime length with a 7-smooth n - 1: Rader's algorithm
@@ -166,6 +168,13 @@ struct PlanImpl {
           need(core2, len_m);
         }
         break;
+      case CHFFT_KIND_CFFT3D:
+        if (len_l > 0 && len_m > 0 && len_n > 0) {
+          need(core, len_n);
+          need(core2, len_m);
+          need(core3, len_l);
+        }
+        break;
       case CHFFT_KIND_RFFT1D: {
         long long h = len / 2;
         need(core, h);
@@ -215,6 +224,7 @@ struct PlanImpl {
     switch (kind) {
       case CHFFT_KIND_CFFT1D: return (size_t)len;
       case CHFFT_KIND_CFFT2D: return (size_t)(len_m * len_n);
+      case CHFFT_KIND_CFFT3D: return (size_t)(len_l * len_m * len_n);
       case CHFFT_KIND_RFFT1D: return back ? (size_t)(len / 2 + 1) : (size_t)len;
       case CHFFT_KIND_DCT1D: return (size_t)len;
       default: return back ? (size_t)(len / 2) : (size_t)len;
@@ -230,7 +240,7 @@ struct PlanImpl {
   // Bytes per element of the input / output side.
   size_t in_esize(bool back) const {
     switch (kind) {
-      case CHFFT_KIND_CFFT1D: case CHFFT_KIND_CFFT2D: return cplx_bytes(dtype);
+      case CHFFT_KIND_CFFT1D: case CHFFT_KIND_CFFT2D: case CHFFT_KIND_CFFT3D: return cplx_bytes(dtype);
       case CHFFT_KIND_RFFT1D: return back ? cplx_bytes(dtype) : real_bytes(dtype);
       default: return real_bytes(dtype);
     }
@@ -241,7 +251,9 @@ struct PlanImpl {
   }
 
   double scale_value(ScaleKind k) const {
-    double n = kind == CHFFT_KIND_CFFT2D ? (double)len_m * (double)len_n : (double)len;
+    double n = kind == CHFFT_KIND_CFFT2D   ? (double)len_m * (double)len_n
+               : kind == CHFFT_KIND_CFFT3D ? (double)len_l * (double)len_m * (double)len_n
+                                           : (double)len;
     switch (k) {
       case S_ONE: return 1.0;
       case S_UNITARY: return 1.0 / std::sqrt(n);
@@ -359,6 +371,34 @@ struct PlanImpl {
         b.in_dist = b.out_dist = len_m * len_n;
         b.ncols = (int)len_n;
         dispatch<T>(Kernel::COLS, core2, g, b, (unsigned)(batch * b.tiles_per_tr), batch * len_m * len_n, s);
+        return;
+      }
+      case CHFFT_KIND_CFFT3D: {
+        if (len_l == 0 || len_m == 0 || len_n == 0) return;
+        // Rows of N into d_out, then the M axis (column tiles of each of the
+        // batch x L planes, in place), then the L axis (column tiles over
+        // the M x N columns of each volume, in place, with the scale).
+        a.in_dist = a.out_dist = len_n;
+        a.scale = 1.0;
+        launch<T>(Kernel::C2C, core, a, batch * len_l * len_m, s);
+        auto columns = [&](const Core& c, long long count, long long ncols, long long rows, double scale) {
+          KArgs b{};
+          b.core = c.desc();
+          Geo g = col_geo(c, (int)ncols, opts.fs_tpb, opts);
+          b.tpb = g.tpb;
+          b.ld = g.ld;
+          b.back = a.back;
+          b.count = count;
+          b.tiles_per_tr = (ncols + g.tpb - 1) / g.tpb;
+          b.in = d_out;
+          b.out = d_out;
+          b.scale = scale;
+          b.in_dist = b.out_dist = rows * ncols;
+          b.ncols = (int)ncols;
+          dispatch<T>(Kernel::COLS, c, g, b, (unsigned)(count * b.tiles_per_tr), count * rows * ncols, s);
+        };
+        columns(core2, batch * len_l, len_n, len_m, 1.0);
+        columns(core3, batch, len_m * len_n, len_l, sc);
         return;
       }
       case CHFFT_KIND_RFFT1D:

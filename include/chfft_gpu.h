@@ -47,12 +47,13 @@ typedef enum chfft_kind {
   CHFFT_KIND_CFFT2D = 1,
   CHFFT_KIND_RFFT1D = 2,
   CHFFT_KIND_DCT1D = 3,
-  CHFFT_KIND_MDCT1D = 4
+  CHFFT_KIND_MDCT1D = 4,
+  CHFFT_KIND_CFFT3D = 5 /* no counterpart in the reference: a native 3-D layout */
 } chfft_kind;
 
 /* The reference's method names (src/cfft1d.rs:270-455 and the same names
  * on the other types). Each type accepts the subset it defines:
- *   CFft1D: all 12;  CFft2D: FORWARD..BACKWARDU (no BACKWARDN, no in-place);
+ *   CFft1D: all 12;  CFft2D and CFft3D: FORWARD..BACKWARDU (no BACKWARDN, no in-place);
  *   RFft1D: FORWARD..BACKWARDN;  Dct1D: FORWARD..FORWARDN;
  *   Mdct1D: FORWARD, FORWARDU, BACKWARD, BACKWARDU. */
 typedef enum chfft_method {
@@ -87,6 +88,13 @@ typedef struct chfft_plan_s* chfft_plan;
 CHFFT_API int chfft_cfft1d_create(int dtype, size_t len, chfft_plan* out);
 /* CFft2D::with_len (src/cfft2d.rs:93-103); 0 x 0 gives CFft2D::new. */
 CHFFT_API int chfft_cfft2d_create(int dtype, size_t len_m, size_t len_n, chfft_plan* out);
+/* 3-D complex transform of a row-major len_l x len_m x len_n array. No
+ * counterpart in the reference (chfft stops at CFft2D, src/cfft2d.rs); it
+ * extends CFft2D's semantics by one axis: the same methods and scales
+ * (1/(L M N) for BACKWARD), rows of len_n first, then the len_m axis, then
+ * the len_l axis. Each axis length must fit one CTA's engine (mixed radix
+ * or Bluestein), as for CFft2D. 0 x 0 x 0 gives an empty plan. */
+CHFFT_API int chfft_cfft3d_create(int dtype, size_t len_l, size_t len_m, size_t len_n, chfft_plan* out);
 /* RFft1D::new (src/rfft1d.rs:73-90): odd len -> CHFFT_EINVAL_LEN. */
 CHFFT_API int chfft_rfft1d_create(int dtype, size_t len, chfft_plan* out);
 /* Dct1D::new (src/dct1d.rs:53-62): odd len -> CHFFT_EINVAL_LEN. */
@@ -121,6 +129,10 @@ CHFFT_API int chfft_execute(chfft_plan plan, int method, const void* src, size_t
 /* CFft2D::method(&rows) on a row-major len_m x len_n host array (re-plans
  * when the shape differs from the plan's). */
 CHFFT_API int chfft_execute_2d(chfft_plan plan, int method, const void* src, size_t len_m, size_t len_n,
+                               void* dst);
+/* CFft3D on a row-major len_l x len_m x len_n host array (re-plans when the
+ * shape differs from the plan's; an empty shape returns at once). */
+CHFFT_API int chfft_execute_3d(chfft_plan plan, int method, const void* src, size_t len_l, size_t len_m, size_t len_n,
                                void* dst);
 /* `batch` independent transforms on host memory, each laid out back to back
  * (input and output strides are the per-transform element counts). */
@@ -256,6 +268,7 @@ typedef struct chfft_plan_info {
    * forces the cluster size). */
   int cluster_ctas;
   size_t cluster_n1, cluster_n2, cluster_max_batch;
+  size_t len_l; /* CFft3D: the outer axis (len_m, len_n the others) */
 } chfft_plan_info;
 
 CHFFT_API int chfft_plan_get_info(chfft_plan plan, chfft_plan_info* info);
