@@ -880,7 +880,7 @@ bool cluster_code(long long n, unsigned long long* code, int* np, int* min_r) {
 }
 }  // namespace
 
-bool ClusterCore::build(long long n_, int dtype_, cudaStream_t s) {
+bool ClusterCore::build(long long n_, int dtype_, cudaStream_t s, bool beyond_cta) {
   release();
   // CHFFT_CLUSTER: 0 off, 8 or 16 forces the cluster size; unset: the size
   // below. Both dtypes (f32 one-CTA rows are latency-bound at these batches
@@ -893,6 +893,12 @@ bool ClusterCore::build(long long n_, int dtype_, cudaStream_t s) {
     if (force != 8 && force != 16) force = 0;
   }
   if (n_ < 64 || n_ > (1LL << 20)) return false;
+  // Against the four-step launches (GB300, forward + backward per graph
+  // replay): f32 32768 at batches 1-4 32.8 against 36.8-38.9 us but 51
+  // against 20 at batch 9, 65536 55 against 34.5; f64 16384 51 against 74
+  // at batches 1-4, 96 against 74 at 9, 32768 even. So beyond one CTA the
+  // form takes f32 up to 32768 and f64 up to 16384, at most 4 transforms.
+  if (beyond_cta && !force && n_ > (dtype_ == 0 ? 32768 : 16384)) return false;
   const size_t cbytes = cplx_bytes(dtype_);
   struct Pick {
     int n1 = 0, n2 = 0, c = 0, th = 0, lda = 0, ldb = 0, tsz = 0, npa = 0, npb = 0;
@@ -951,6 +957,7 @@ bool ClusterCore::build(long long n_, int dtype_, cudaStream_t s) {
     // Batches up to one cluster per csize SMs: every transform's cluster
     // runs at once (CHFFT_CLUSTER_MAX_BATCH overrides).
     max_batch = std::max(1, num_sms() / csize);
+    if (beyond_cta) max_batch = std::min<long long>(max_batch, 4);
     if (const char* e = std::getenv("CHFFT_CLUSTER_MAX_BATCH")) max_batch = std::max(0LL, std::atoll(e));
     tab_a.ensure(std::max<size_t>(1, (size_t)(npa - 1) * n1) * cbytes);
     tab_b.ensure(std::max<size_t>(1, (size_t)(npb - 1) * n2) * cbytes);

@@ -169,8 +169,10 @@ struct ClusterCore {
   DevBuf blk[kScales];
   // Host-mapped error word: 7 when a CTA's wait for its rows gave up.
   HostWord err;
-  // false: no split, no cluster shape that launches, or CHFFT_CLUSTER=0.
-  bool build(long long n, int dtype, cudaStream_t s);
+  // false: no split, no cluster shape that launches, CHFFT_CLUSTER=0, or
+  // (beyond_cta: the plan's own path is the four-step one) a length where
+  // the four-step launches are faster.
+  bool build(long long n, int dtype, cudaStream_t s, bool beyond_cta = false);
   void release() {
     n = 0;
     max_batch = 0;

@@ -159,7 +159,7 @@ struct PlanImpl {
           use_big = true;
         }
         clus.release();
-        if (!use_rader && !(one_cta && core.blue) && !(use_big && big.blue)) clus.build(len, dtype, s);
+        if (!use_rader && !(one_cta && core.blue) && !(use_big && big.blue)) clus.build(len, dtype, s, use_big);
         break;
       }
       case CHFFT_KIND_CFFT2D:
