@@ -954,9 +954,13 @@ bool ClusterCore::build(long long n_, int dtype_, cudaStream_t s, bool beyond_ct
     code_a = best.ca;
     code_b = best.cb;
     smem = best.smem;
-    // Batches up to one cluster per csize SMs: every transform's cluster
-    // runs at once (CHFFT_CLUSTER_MAX_BATCH overrides).
-    max_batch = std::max(1, num_sms() / csize);
+    // Batches up to 2^18 (f64) or 2^16 (f32) elements, at most one
+    // transform per SM: measured crossovers against the one-CTA rows
+    // (GB300, forward + backward per graph replay): f64 4096 96 against
+    // 106 us at batch 76 but 174 against 106 at 152, 1024 43 against 55 at
+    // 152; f32 4096 20.5 against 20.4 at 38, 1024 14.3 against 14.3 at 76,
+    // 256 12.2 against 14.3 at 152 (CHFFT_CLUSTER_MAX_BATCH overrides).
+    max_batch = std::max<long long>(1, std::min<long long>(num_sms(), (dtype_ == 0 ? (1LL << 16) : (1LL << 18)) / n_));
     if (beyond_cta) max_batch = std::min<long long>(max_batch, 4);
     if (const char* e = std::getenv("CHFFT_CLUSTER_MAX_BATCH")) max_batch = std::max(0LL, std::atoll(e));
     tab_a.ensure(std::max<size_t>(1, (size_t)(npa - 1) * n1) * cbytes);
