@@ -92,6 +92,7 @@ def lib() -> ctypes.CDLL:
         "chfft_execute": [vp, i, vp, sz, vp, sz],
         "chfft_execute_2d": [vp, i, vp, sz, sz, vp],
         "chfft_execute_3d": [vp, i, vp, sz, sz, sz, vp],
+        "chfft_execute_device_split": [vp, i, vp, vp, vp, vp, sz, vp],
         "chfft_execute_batch": [vp, i, vp, vp, sz],
         "chfft_execute_device": [vp, i, vp, vp, sz, vp],
         "chfft_plan_wait": [vp, vp],
@@ -206,6 +207,13 @@ class _Plan:
         _check(lib().chfft_execute_batch(self._h, METHODS[method], _ptr(src), _ptr(out), batch))
         del info
         return out
+
+    def execute_device_split(self, method: str, d_re: int, d_im: int, d_out_re: int, d_out_im: int, batch: int,
+                             stream: int = 0):
+        """CFft1D on split-complex device arrays (real / imaginary parts apart)."""
+        _check(lib().chfft_execute_device_split(self._h, METHODS[method], ctypes.c_void_p(d_re), ctypes.c_void_p(d_im),
+                                                ctypes.c_void_p(d_out_re), ctypes.c_void_p(d_out_im), batch,
+                                                ctypes.c_void_p(stream)))
 
     def execute_device(self, method: str, d_src: int, d_dst: int, batch: int, stream: int = 0):
         """`batch` transforms on device pointers, enqueued on a CUDA stream handle."""

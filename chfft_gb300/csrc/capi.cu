@@ -274,6 +274,19 @@ int chfft_execute_device(chfft_plan plan, int method, const void* d_src, void* d
   });
 }
 
+int chfft_execute_device_split(chfft_plan plan, int method, const void* d_src_re, const void* d_src_im,
+                               void* d_dst_re, void* d_dst_im, size_t batch, void* stream) {
+  if (!plan) return chfft::set_error(CHFFT_EINVAL, "null plan");
+  PlanImpl& p = plan->impl;
+  chfft::MethodSpec ms = chfft::method_spec(p.kind, method);
+  if (!ms.ok) return chfft::set_error(CHFFT_EINVAL, "method not offered by this type");
+  if (batch && (!d_src_re || !d_src_im || !d_dst_re || !d_dst_im)) return chfft::set_error(CHFFT_EINVAL, "null buffer");
+  return guarded([&]() -> int {
+    p.exec_split(ms, d_src_re, d_src_im, d_dst_re, d_dst_im, (long long)batch, static_cast<cudaStream_t>(stream));
+    return (int)CHFFT_OK;
+  });
+}
+
 int chfft_plan_wait(chfft_plan plan, void* stream) {
   if (!plan) return chfft::set_error(CHFFT_EINVAL, "null plan");
   PlanImpl& p = plan->impl;

@@ -53,6 +53,58 @@ __global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_c2c(cons
   CoreT::run(a.core, a.tpb, sm, ld, st);
 }
 
+// ---------------------------------------------------------------- rows, split complex
+// The same rows with real and imaginary parts in separate arrays (a native
+// layout the reference does not offer; chfft takes interleaved
+// Complex<T>, src/cfft1d.rs:270). KArgs: in / aux0 the input's real /
+// imaginary parts, out / aux1 the output's.
+template <typename C>
+struct SplitLoad {
+  using R = typename Real<C>::type;
+  const R* re;
+  const R* im;
+  long long dist;
+  int nvalid;
+  R scale;
+  int back;
+  __device__ __forceinline__ C load(int t, int i) const {
+    if (t >= nvalid) return czero<C>();
+    const long long k = (long long)t * dist + i;
+    const C v = mk(re[k] * scale, im[k] * scale);
+    return back ? cconj(v) : v;
+  }
+};
+
+template <typename C>
+struct SplitStore {
+  using R = typename Real<C>::type;
+  R* re;
+  R* im;
+  long long dist;
+  int nvalid;
+  int back;
+  __device__ __forceinline__ void store(int t, int i, C v) const {
+    if (t >= nvalid) return;
+    const long long k = (long long)t * dist + i;
+    re[k] = v.x;
+    im[k] = back ? -v.y : v.y;
+  }
+};
+
+template <typename T, class CoreT>
+__global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_c2c_split(const KArgs a) {
+  using C = cx_t<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
+  const long long t0 = (long long)blockIdx.x * a.tpb;
+  const int nvalid = (int)min((long long)a.tpb, a.count - t0);
+  SplitLoad<C> ld{(const T*)a.in + t0 * a.in_dist, (const T*)a.aux0 + t0 * a.in_dist, a.in_dist, nvalid, (T)a.scale,
+                  a.back};
+  SplitStore<C> st{(T*)a.out + t0 * a.out_dist, (T*)const_cast<void*>(a.aux1) + t0 * a.out_dist, a.out_dist, nvalid,
+                   a.back};
+  CoreT::run(a.core, a.tpb, sm, ld, st);
+}
+
 // ---------------------------------------------------------------- rows, Rader
 // A prime length N whose N - 1 = L is 7-smooth (N = 1009: L = 2^4 3^2 7)
 // by Rader's algorithm instead of Chirp-Z (src/chirpz.rs:87-146 computes
@@ -455,6 +507,7 @@ cudaError_t launch_complex(Kernel which, bool blue, bool k1, const KArgs& a, uns
         : (k1 ? K<T, DynCore<false, TMINOR, true, true>> : K<T, DynCore<false, TMINOR, true, false>>))
   switch (which) {
     case Kernel::C2C: fn = CHFFT_PICK(k_c2c, false); break;
+    case Kernel::C2C_SPLIT: fn = CHFFT_PICK(k_c2c_split, false); break;
     case Kernel::C2C_RADER:
       fn = k1 ? k_c2c_rader<T, DynCore<false, false, true, true>> : k_c2c_rader<T, DynCore<false, false, true, false>>;
       break;

@@ -426,6 +426,34 @@ struct PlanImpl {
     }
   }
 
+  // CFft1D on split-complex device arrays (re / im separate): the one-CTA
+  // row kernels (library form). Plans beyond one CTA or on Rader's path
+  // are refused.
+  void exec_split(const MethodSpec& ms, const void* in_re, const void* in_im, void* out_re, void* out_im,
+                  long long batch, cudaStream_t s) {
+    if (kind != CHFFT_KIND_CFFT1D || use_big || use_rader || len < 2)
+      throw Fail{CHFFT_EUNSUPPORTED, "split-complex execution needs a CFft1D plan of 2 or more points within one CTA"};
+    if (batch <= 0) return;
+    KArgs a{};
+    a.in = in_re;
+    a.aux0 = in_im;
+    a.out = out_re;
+    a.aux1 = out_im;
+    a.scale = scale_value(ms.scale);
+    a.back = ms.back ? 1 : 0;
+    a.in_dist = a.out_dist = len;
+    Geo g = row_geo(core, batch, opts);
+    a.core = core.desc();
+    a.tpb = g.tpb;
+    a.ld = g.ld;
+    a.count = batch;
+    const unsigned blocks = (unsigned)((batch + g.tpb - 1) / g.tpb);
+    if (dtype == CHFFT_F32)
+      CHFFT_CUDA(launch_kernel<float>(Kernel::C2C_SPLIT, core.blue, g.k1, a, blocks, g.threads, g.smem, s));
+    else
+      CHFFT_CUDA(launch_kernel<double>(Kernel::C2C_SPLIT, core.blue, g.k1, a, blocks, g.threads, g.smem, s));
+  }
+
   // Throws CHFFT_ETIMEOUT when a bounded device-side wait of this plan's
   // kernels gave up since the last check (the host-mapped word the
   // pipelined four-step launch sets). Call after a synchronisation.

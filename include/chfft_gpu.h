@@ -143,6 +143,15 @@ CHFFT_API int chfft_execute_batch(chfft_plan plan, int method, const void* src, 
 CHFFT_API int chfft_execute_device(chfft_plan plan, int method, const void* d_src, void* d_dst, size_t batch,
                                    void* stream);
 
+/* CFft1D on split-complex device arrays: real and imaginary parts in
+ * separate arrays of the working dtype, `batch` transforms back to back in
+ * each (no counterpart in the reference, whose Complex<T> is interleaved,
+ * src/cfft1d.rs:270). Any CFft1D method; source and destination arrays may
+ * be the same. Plans whose length fits one CTA (algorithm 0 or 1 in
+ * chfft_plan_info); others get CHFFT_EUNSUPPORTED. */
+CHFFT_API int chfft_execute_device_split(chfft_plan plan, int method, const void* d_src_re, const void* d_src_im,
+                                         void* d_dst_re, void* d_dst_im, size_t batch, void* stream);
+
 /* Waits for `stream`, then reports CHFFT_ETIMEOUT if a bounded device-side
  * wait in one of this plan's launches gave up since the last check (the
  * launch then returned without hanging and its output is incomplete; the
