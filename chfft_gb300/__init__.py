@@ -93,6 +93,7 @@ def lib() -> ctypes.CDLL:
         "chfft_execute_2d": [vp, i, vp, sz, sz, vp],
         "chfft_execute_3d": [vp, i, vp, sz, sz, sz, vp],
         "chfft_execute_device_split": [vp, i, vp, vp, vp, vp, sz, vp],
+        "chfft_execute_device_strided": [vp, i, vp, sz, sz, vp, sz, sz, sz, vp],
         "chfft_execute_batch": [vp, i, vp, vp, sz],
         "chfft_execute_device": [vp, i, vp, vp, sz, vp],
         "chfft_plan_wait": [vp, vp],
@@ -214,6 +215,13 @@ class _Plan:
         _check(lib().chfft_execute_device_split(self._h, METHODS[method], ctypes.c_void_p(d_re), ctypes.c_void_p(d_im),
                                                 ctypes.c_void_p(d_out_re), ctypes.c_void_p(d_out_im), batch,
                                                 ctypes.c_void_p(stream)))
+
+    def execute_device_strided(self, method: str, d_src: int, istride: int, idist: int, d_dst: int, ostride: int,
+                               odist: int, batch: int, stream: int = 0):
+        """CFft1D on strided device layouts (element i of transform t at t * dist + i * stride)."""
+        _check(lib().chfft_execute_device_strided(self._h, METHODS[method], ctypes.c_void_p(d_src), istride, idist,
+                                                  ctypes.c_void_p(d_dst), ostride, odist, batch,
+                                                  ctypes.c_void_p(stream)))
 
     def execute_device(self, method: str, d_src: int, d_dst: int, batch: int, stream: int = 0):
         """`batch` transforms on device pointers, enqueued on a CUDA stream handle."""

@@ -287,6 +287,20 @@ int chfft_execute_device_split(chfft_plan plan, int method, const void* d_src_re
   });
 }
 
+int chfft_execute_device_strided(chfft_plan plan, int method, const void* d_src, size_t istride, size_t idist,
+                                 void* d_dst, size_t ostride, size_t odist, size_t batch, void* stream) {
+  if (!plan) return chfft::set_error(CHFFT_EINVAL, "null plan");
+  PlanImpl& p = plan->impl;
+  chfft::MethodSpec ms = chfft::method_spec(p.kind, method);
+  if (!ms.ok) return chfft::set_error(CHFFT_EINVAL, "method not offered by this type");
+  if (batch && (!d_src || !d_dst)) return chfft::set_error(CHFFT_EINVAL, "null buffer");
+  return guarded([&]() -> int {
+    p.exec_strided(ms, d_src, (long long)istride, (long long)idist, d_dst, (long long)ostride, (long long)odist,
+                   (long long)batch, static_cast<cudaStream_t>(stream));
+    return (int)CHFFT_OK;
+  });
+}
+
 int chfft_plan_wait(chfft_plan plan, void* stream) {
   if (!plan) return chfft::set_error(CHFFT_EINVAL, "null plan");
   PlanImpl& p = plan->impl;

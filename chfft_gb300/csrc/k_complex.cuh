@@ -105,6 +105,49 @@ __global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_c2c_spli
   CoreT::run(a.core, a.tpb, sm, ld, st);
 }
 
+// ---------------------------------------------------------------- rows, strided
+// Element i of transform t at t * dist + i * stride (complex elements), for
+// input and output separately (a native layout beyond the reference's
+// contiguous slices: matrix columns, padded rows, interleaved channels).
+// KArgs: in_dist / out_dist the distances, ncols / n_user the input /
+// output strides.
+template <typename C>
+struct StridedLoad {
+  const C* in;
+  long long dist, stride;
+  int nvalid;
+  typename Real<C>::type scale;
+  int back;
+  __device__ __forceinline__ C load(int t, int i) const {
+    if (t >= nvalid) return czero<C>();
+    const C v = cscale(in[(long long)t * dist + (long long)i * stride], scale);
+    return back ? cconj(v) : v;
+  }
+};
+
+template <typename C>
+struct StridedStore {
+  C* out;
+  long long dist, stride;
+  int nvalid;
+  int back;
+  __device__ __forceinline__ void store(int t, int i, C v) const {
+    if (t < nvalid) out[(long long)t * dist + (long long)i * stride] = back ? cconj(v) : v;
+  }
+};
+
+template <typename T, class CoreT>
+__global__ void __launch_bounds__(CoreT::kThreads, CoreT::kMinBlocks) k_c2c_strided(const KArgs a) {
+  using C = cx_t<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const auto sm = CoreT::template tile<C>(smem_raw, a.ld);
+  const long long t0 = (long long)blockIdx.x * a.tpb;
+  const int nvalid = (int)min((long long)a.tpb, a.count - t0);
+  StridedLoad<C> ld{(const C*)a.in + t0 * a.in_dist, a.in_dist, (long long)a.ncols, nvalid, (T)a.scale, a.back};
+  StridedStore<C> st{(C*)a.out + t0 * a.out_dist, a.out_dist, (long long)a.n_user, nvalid, a.back};
+  CoreT::run(a.core, a.tpb, sm, ld, st);
+}
+
 // ---------------------------------------------------------------- rows, Rader
 // A prime length N whose N - 1 = L is 7-smooth (N = 1009: L = 2^4 3^2 7)
 // by Rader's algorithm instead of Chirp-Z (src/chirpz.rs:87-146 computes
@@ -508,6 +551,7 @@ cudaError_t launch_complex(Kernel which, bool blue, bool k1, const KArgs& a, uns
   switch (which) {
     case Kernel::C2C: fn = CHFFT_PICK(k_c2c, false); break;
     case Kernel::C2C_SPLIT: fn = CHFFT_PICK(k_c2c_split, false); break;
+    case Kernel::C2C_STRIDED: fn = CHFFT_PICK(k_c2c_strided, false); break;
     case Kernel::C2C_RADER:
       fn = k1 ? k_c2c_rader<T, DynCore<false, false, true, true>> : k_c2c_rader<T, DynCore<false, false, true, false>>;
       break;

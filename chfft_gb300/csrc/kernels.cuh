@@ -46,6 +46,7 @@ enum class Kernel : int {
   ROWS_BB = 10, // four-step Bluestein middle pass (k_rows_bb)
   C2C_RADER = 11, // rows of a prime length by Rader's algorithm (k_c2c_rader)
   C2C_SPLIT = 12, // rows with separate real / imaginary arrays (k_c2c_split, library kernels only)
+  C2C_STRIDED = 13, // rows with element strides and transform distances (k_c2c_strided, library kernels only)
 };
 
 // Four-step geometry of a length-N FFT beyond one CTA, N = n1 * n2.

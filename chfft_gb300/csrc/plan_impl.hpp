@@ -4,6 +4,7 @@
 #pragma once
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -452,6 +453,37 @@ struct PlanImpl {
       CHFFT_CUDA(launch_kernel<float>(Kernel::C2C_SPLIT, core.blue, g.k1, a, blocks, g.threads, g.smem, s));
     else
       CHFFT_CUDA(launch_kernel<double>(Kernel::C2C_SPLIT, core.blue, g.k1, a, blocks, g.threads, g.smem, s));
+  }
+
+  // CFft1D on strided device layouts: element i of transform t at
+  // t * dist + i * stride (complex elements, input and output apart), the
+  // one-CTA row kernels (library form).
+  void exec_strided(const MethodSpec& ms, const void* in, long long istride, long long idist, void* out,
+                    long long ostride, long long odist, long long batch, cudaStream_t s) {
+    if (kind != CHFFT_KIND_CFFT1D || use_big || use_rader || len < 2)
+      throw Fail{CHFFT_EUNSUPPORTED, "strided execution needs a CFft1D plan of 2 or more points within one CTA"};
+    if (istride < 1 || ostride < 1 || istride > INT_MAX || ostride > INT_MAX || idist < 0 || odist < 0)
+      throw Fail{CHFFT_EINVAL, "strides must be in [1, 2^31) and distances non-negative"};
+    if (batch <= 0) return;
+    KArgs a{};
+    a.in = in;
+    a.out = out;
+    a.ncols = (int)istride;
+    a.n_user = (int)ostride;
+    a.in_dist = idist;
+    a.out_dist = odist;
+    a.scale = scale_value(ms.scale);
+    a.back = ms.back ? 1 : 0;
+    Geo g = row_geo(core, batch, opts);
+    a.core = core.desc();
+    a.tpb = g.tpb;
+    a.ld = g.ld;
+    a.count = batch;
+    const unsigned blocks = (unsigned)((batch + g.tpb - 1) / g.tpb);
+    if (dtype == CHFFT_F32)
+      CHFFT_CUDA(launch_kernel<float>(Kernel::C2C_STRIDED, core.blue, g.k1, a, blocks, g.threads, g.smem, s));
+    else
+      CHFFT_CUDA(launch_kernel<double>(Kernel::C2C_STRIDED, core.blue, g.k1, a, blocks, g.threads, g.smem, s));
   }
 
   // Throws CHFFT_ETIMEOUT when a bounded device-side wait of this plan's

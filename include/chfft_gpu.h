@@ -152,6 +152,17 @@ CHFFT_API int chfft_execute_device(chfft_plan plan, int method, const void* d_sr
 CHFFT_API int chfft_execute_device_split(chfft_plan plan, int method, const void* d_src_re, const void* d_src_im,
                                          void* d_dst_re, void* d_dst_im, size_t batch, void* stream);
 
+/* CFft1D on strided device layouts: element i of transform t at
+ * t * idist + i * istride of d_src (complex elements) and t * odist +
+ * i * ostride of d_dst: matrix columns, padded rows, interleaved channels
+ * (no counterpart in the reference, which takes contiguous slices). Any
+ * CFft1D method; strides in [1, 2^31). d_src == d_dst only with the same
+ * layout on both sides, and the layouts must not map two elements of the
+ * batch to one address. One-CTA lengths; others get CHFFT_EUNSUPPORTED. */
+CHFFT_API int chfft_execute_device_strided(chfft_plan plan, int method, const void* d_src, size_t istride,
+                                           size_t idist, void* d_dst, size_t ostride, size_t odist, size_t batch,
+                                           void* stream);
+
 /* Waits for `stream`, then reports CHFFT_ETIMEOUT if a bounded device-side
  * wait in one of this plan's launches gave up since the last check (the
  * launch then returned without hanging and its output is incomplete; the
