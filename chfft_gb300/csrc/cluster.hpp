@@ -22,6 +22,15 @@ cudaError_t cluster_launch(const void* fn, const clus::ClusterArgs& a, long long
 cudaError_t cluster_pass_tables(int dtype, int n, unsigned long long code, int np, void* out, cudaStream_t s);
 // The four-step twiddles w_n^(n2 k1) x scale at n2 * n1 + k1.
 cudaError_t cluster_block_table(int dtype, long long n, int n1, double scale, void* out, cudaStream_t s);
+// RFft1D around a cluster FFT of the half length h (k_cluster.cu): the
+// split of batch forward cores z (h complex each) into out (h + 1 each),
+// times scale; the merge of batch inputs (h + 1 each) into z (h each),
+// times s2, for a backward (conjugating) core. Programmatic dependent
+// launches on s.
+cudaError_t rfft_split(int dtype, const void* z, void* out, const void* coef, int h, long long batch, double scale,
+                       cudaStream_t s);
+cudaError_t rfft_merge(int dtype, const void* in, void* z, const void* bcoef, int h, long long batch, double s2,
+                       cudaStream_t s);
 // Clusters of this shape the current device can hold at once (0: none, the
 // shape cannot launch).
 int cluster_max_active(const void* fn, int csize, int threads, size_t smem);

@@ -122,7 +122,100 @@ __global__ void k_block_table(long long n, int n1, double scale, void* out) {
   reinterpret_cast<C*>(out)[k] = mk((T)(c * scale), (T)(sn * scale));
 }
 
+// RFft1D around the cluster FFT of the half length h: the split after a
+// forward core (src/rfft1d.rs:136-148: X_i = Z_i - x, X_{h-i} = Z_{h-i} +
+// conj x, x = coef_i (Z_i - conj Z_{h-i}); DC, Nyquist and N/4 bins from
+// item 0), times the method's scale; and the merge before a backward core
+// (src/rfft1d.rs:132-145), times 2 scale (the core then runs the conjugated
+// forward FFT). Thread (t, i < ceil(N/4)) of the grid. Launched after or
+// before a cluster kernel with programmatic dependent launch: each waits for
+// the kernels before it before reading.
+template <typename T>
+__global__ void k_rfft_split(const cx_t<T>* z, cx_t<T>* out, const cx_t<T>* coef, int h, long long batch, T scale) {
+  using C = cx_t<T>;
+  clus::allow_dependents();
+  clus::wait_prerequisites();
+  const int qlen = (2 * h + 3) >> 2;
+  const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= batch * qlen) return;
+  const long long t = w / qlen;
+  const int i = (int)(w - t * qlen);
+  const C* zt = z + t * h;
+  C* o = out + t * (h + 1);
+  if (i == 0) {
+    const C z0 = zt[0];
+    o[0] = mk((z0.x + z0.y) * scale, T(0));
+    o[h] = mk((z0.x - z0.y) * scale, T(0));
+    if (((2 * h) & 3) == 0) o[qlen] = cscale(cconj(zt[qlen]), scale);
+  } else {
+    const C zi = zt[i], zh = zt[h - i];
+    const C x = cmul(coef[i], csub(zi, cconj(zh)));
+    o[i] = cscale(csub(zi, x), scale);
+    o[h - i] = cscale(cadd(zh, cconj(x)), scale);
+  }
+}
+
+template <typename T>
+__global__ void k_rfft_merge(const cx_t<T>* in, cx_t<T>* z, const cx_t<T>* bcoef, int h, long long batch, T s2) {
+  using C = cx_t<T>;
+  clus::allow_dependents();
+  clus::wait_prerequisites();
+  const int qlen = (2 * h + 3) >> 2;
+  const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= batch * qlen) return;
+  const long long t = w / qlen;
+  const int i = (int)(w - t * qlen);
+  const C* s = in + t * (h + 1);
+  C* zt = z + t * h;
+  if (i == 0) {
+    const C s0 = s[0], sh = s[h];
+    zt[0] = mk((s0.x + sh.x) * T(0.5) * s2, (s0.x - sh.x) * T(0.5) * s2);
+    if (((2 * h) & 3) == 0) zt[qlen] = cscale(cconj(s[qlen]), s2);
+  } else {
+    const C si = s[i], sh = s[h - i];
+    const C x = cmul(bcoef[i], csub(si, cconj(sh)));
+    zt[i] = cscale(csub(si, x), s2);
+    zt[h - i] = cscale(cadd(sh, cconj(x)), s2);
+  }
+}
+
+template <typename K, typename... Args>
+cudaError_t pdl_launch(K kernel, unsigned blocks, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(blocks, 1, 1);
+  cfg.blockDim = dim3(256, 1, 1);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 }  // namespace
+
+cudaError_t rfft_split(int dtype, const void* z, void* out, const void* coef, int h, long long batch, double scale,
+                       cudaStream_t s) {
+  const long long items = batch * ((2LL * h + 3) >> 2);
+  const unsigned blocks = (unsigned)((items + 255) / 256);
+  if (dtype == 0)
+    return pdl_launch(k_rfft_split<float>, blocks, s, static_cast<const float2*>(z), static_cast<float2*>(out),
+                      static_cast<const float2*>(coef), h, batch, (float)scale);
+  return pdl_launch(k_rfft_split<double>, blocks, s, static_cast<const double2*>(z), static_cast<double2*>(out),
+                    static_cast<const double2*>(coef), h, batch, scale);
+}
+
+cudaError_t rfft_merge(int dtype, const void* in, void* z, const void* bcoef, int h, long long batch, double s2,
+                       cudaStream_t s) {
+  const long long items = batch * ((2LL * h + 3) >> 2);
+  const unsigned blocks = (unsigned)((items + 255) / 256);
+  if (dtype == 0)
+    return pdl_launch(k_rfft_merge<float>, blocks, s, static_cast<const float2*>(in), static_cast<float2*>(z),
+                      static_cast<const float2*>(bcoef), h, batch, (float)s2);
+  return pdl_launch(k_rfft_merge<double>, blocks, s, static_cast<const double2*>(in), static_cast<double2*>(z),
+                    static_cast<const double2*>(bcoef), h, batch, s2);
+}
 
 cudaError_t cluster_pass_tables(int dtype, int n, unsigned long long code, int np, void* out, cudaStream_t s) {
   PassTab pt{};

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/chfft_gpu.h"
+#include "cluster.hpp"
 #include "jit.hpp"
 #include "plan.hpp"
 namespace chfft {
@@ -183,6 +184,9 @@ struct PlanImpl {
         aux1.ensure(h * cb);
         gen(Table::RCOEF, len, h, aux0.p);
         gen(Table::RBCOEF, len, h, aux1.p);
+        // small batches: the half-length FFT on a cluster, split / merge apart
+        clus.release();
+        if (!core.blue) clus.build(h, dtype, s);
         break;
       }
       case CHFFT_KIND_DCT1D: {
@@ -403,6 +407,21 @@ struct PlanImpl {
         return;
       }
       case CHFFT_KIND_RFFT1D:
+        if (clus.n && batch <= clus.max_batch && opts.tc <= 0) {
+          // The half-length FFT on a cluster with scale 1, the split (forward)
+          // or the merge (backward, times 2 scale) in its own launch.
+          const int h = (int)(len / 2);
+          work.ensure((size_t)batch * h * cplx_bytes(dtype));
+          if (!ms.back) {
+            if (clus.exec(d_in, work.p, batch, false, 1.0, s)) {
+              CHFFT_CUDA(rfft_split(dtype, work.p, d_out, aux0.p, h, batch, sc, s));
+              return;
+            }
+          } else {
+            CHFFT_CUDA(rfft_merge(dtype, d_in, work.p, aux1.p, h, batch, 2.0 * sc, s));
+            if (clus.exec(work.p, d_out, batch, true, 1.0, s)) return;
+          }
+        }
         a.aux0 = ms.back ? aux1.p : aux0.p;
         a.in_dist = ms.back ? len / 2 + 1 : len;
         a.out_dist = ms.back ? len : len / 2 + 1;

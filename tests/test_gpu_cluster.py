@@ -182,3 +182,32 @@ def test_compile_time_and_run_time_shapes_agree(n, static):
         y = p.execute_batch("forward", x[:b])
         assert rel(y, np.fft.fft(x[:b], axis=-1)) <= 1e-12
         assert rel(p.execute_batch("backward", y), x[:b]) <= 1e-12
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+@pytest.mark.parametrize("n", [128, 1024, 8192, 2304])
+def test_rfft1d_cluster_form_matches_oracle(dt, n):
+    """RFft1D runs its half-length FFT on a cluster at small batches (the
+    split / merge in their own launches); every method matches the oracle,
+    and the plan with CHFFT_CLUSTER=0 gives the same spectra."""
+    with env(CHFFT_CLUSTER=None):
+        p = cg.RFft1D(n, dt)
+    assert p.info().cluster_ctas in (8, 16)
+    with env(CHFFT_CLUSTER="0"):
+        q = cg.RFft1D(n, dt)
+    assert q.info().cluster_ctas == 0
+    rng = np.random.default_rng(n)
+    x = rng.uniform(-1, 1, (3, n))
+    xs = x.astype(dt)
+    tol = TOL[dt]
+    for method in ("forward", "forwardu", "forwardn"):
+        y = p.execute_batch(method, xs)
+        ref = np.stack([oracle.rfft1d(xs[i].astype(np.float64), method) for i in range(3)])
+        assert rel(y, ref) <= tol, method
+        assert rel(y, q.execute_batch(method, xs)) <= tol, method
+    spec = np.fft.rfft(xs.astype(np.float64), axis=-1).astype(np.complex128 if dt == np.float64 else np.complex64)
+    for method in ("backward", "backwardu"):
+        z = p.execute_batch(method, spec)
+        ref = np.stack([oracle.rfft1d(spec[i].astype(np.complex128), method) for i in range(3)])
+        assert rel(z, ref) <= tol, method
+    assert rel(p.execute_batch("backward", p.execute_batch("forward", xs)), xs) <= 2 * tol
