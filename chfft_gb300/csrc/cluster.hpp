@@ -31,6 +31,17 @@ cudaError_t rfft_split(int dtype, const void* z, void* out, const void* coef, in
                        cudaStream_t s);
 cudaError_t rfft_merge(int dtype, const void* in, void* z, const void* bcoef, int h, long long batch, double s2,
                        cudaStream_t s);
+// Dct1D / Mdct1D around a cluster FFT: op kDct2 / kDct3 (core N/2), kMdct /
+// kImdct (core N/4, the forward FFT for both). real_pre turns batch inputs
+// into the core's input z (scale and the DCT ortho factor applied as the
+// one-CTA kernels do); real_post turns the core's output into the outputs
+// (DCT-III's core runs backward; the MDCT scale applied here). n is the
+// user length. Programmatic dependent launches on s.
+enum { kDct2 = 0, kDct3 = 1, kMdct = 2, kImdct = 3 };
+cudaError_t real_pre(int dtype, int op, const void* in, void* z, const void* aux0, const void* aux1, int n,
+                     long long batch, double scale, double ortho, cudaStream_t s);
+cudaError_t real_post(int dtype, int op, const void* z, void* out, const void* aux0, const void* aux1, int n,
+                      long long batch, double scale, cudaStream_t s);
 // Clusters of this shape the current device can hold at once (0: none, the
 // shape cannot launch).
 int cluster_max_active(const void* fn, int csize, int threads, size_t smem);

@@ -9,6 +9,7 @@
 
 #include "cluster.hpp"
 #include "k_cluster.cuh"
+#include "k_real.cuh"
 
 namespace chfft {
 namespace {
@@ -179,6 +180,98 @@ __global__ void k_rfft_merge(const cx_t<T>* in, cx_t<T>* z, const cx_t<T>* bcoef
   }
 }
 
+// Dct1D and Mdct1D around a cluster FFT of the core length m (N/2, N/4):
+// the pre- and post-processing of the one-CTA kernels (k_real.cuh), as
+// their own launches on a workspace of m complex per transform. Pointwise
+// steps reuse the kernels' loaders / storers; the paired ones (DCT-II's
+// post-twiddle, DCT-III's merge) restate their loops on global memory.
+template <typename T, class Ld>
+__global__ void k_pre(Ld ld, cx_t<T>* z, int m, long long batch) {
+  clus::allow_dependents();
+  clus::wait_prerequisites();
+  const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= batch * m) return;
+  const long long t = w / m;
+  z[w] = ld.load((int)t, (int)(w - t * m));
+}
+
+template <typename T, class St>
+__global__ void k_post(St st, const cx_t<T>* z, int m, long long batch, int conj_in) {
+  clus::allow_dependents();
+  clus::wait_prerequisites();
+  const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= batch * m) return;
+  const long long t = w / m;
+  const cx_t<T> v = z[w];
+  st.store((int)t, (int)(w - t * m), conj_in ? cconj(v) : v);
+}
+
+// DCT-II post-twiddle with exp(+i pi k / 2N) (src/dct1d.rs:266-289) of the
+// forward core output z (h per transform) into out (N reals each).
+template <typename T>
+__global__ void k_dct2_post(const cx_t<T>* zs, T* out, const cx_t<T>* coef, const cx_t<T>* om, int h,
+                            long long batch) {
+  using C = cx_t<T>;
+  clus::allow_dependents();
+  clus::wait_prerequisites();
+  const int N = 2 * h, q2 = (N + 3) >> 2;
+  const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= batch * q2) return;
+  const long long t = w / q2;
+  const int i = (int)(w - t * q2);
+  const C* z = zs + t * h;
+  T* o = out + t * N;
+  if (i == 0) {
+    const C z0 = z[0];
+    o[0] = z0.x + z0.y;
+    o[h] = (z0.x - z0.y) * om[h].x;
+    if ((N & 3) == 0) {
+      const C x = cmul(z[q2], om[q2]);
+      o[q2] = x.x;
+      o[N - q2] = x.y;
+    }
+  } else {
+    const C zi = z[i];
+    const C wconj = cconj(z[h - i]);
+    const C x = cmul(coef[i], csub(zi, wconj));
+    const C j = cmul(cconj(csub(zi, x)), om[i]);
+    o[i] = j.x;
+    o[N - i] = j.y;
+    const C k = cmul(cadd(wconj, x), om[h - i]);
+    o[h - i] = k.x;
+    o[h + i] = k.y;
+  }
+}
+
+// DCT-III pre-twiddle and merge (src/dct1d.rs:369-391) of the input (N reals
+// per transform) into z (h each) for a backward (conjugating) core: the
+// values the one-CTA kernel's tile holds, conjugated.
+template <typename T>
+__global__ void k_dct3_pre(const T* xs, cx_t<T>* zs, const cx_t<T>* coef, const cx_t<T>* om, int h, long long batch,
+                           T scale, T ortho) {
+  using C = cx_t<T>;
+  clus::allow_dependents();
+  clus::wait_prerequisites();
+  const int N = 2 * h, q = (N + 3) >> 2;
+  const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= batch * q) return;
+  const long long t = w / q;
+  const int i = (int)(w - t * q);
+  const T* x = xs + t * N;
+  C* z = zs + t * h;
+  if (i == 0) {
+    const T zval = x[0] * ortho, hval = x[h] * om[h].x;
+    z[0] = mk((zval + hval) * scale, (zval - hval) * scale);
+    if ((N & 3) == 0) z[q] = cmul(mk(x[q], x[N - q]), cscale(om[q], scale));
+  } else {
+    const C j = cconj(cscale(cmul(mk(x[i], x[N - i]), om[i]), scale));
+    const C k = cscale(cmul(mk(x[h - i], x[h + i]), om[h - i]), scale);
+    const C xx = cmul(coef[i], csub(j, k));
+    z[i] = csub(j, xx);
+    z[h - i] = cconj(cadd(k, xx));
+  }
+}
+
 template <typename K, typename... Args>
 cudaError_t pdl_launch(K kernel, unsigned blocks, cudaStream_t s, Args... args) {
   cudaLaunchConfig_t cfg{};
@@ -215,6 +308,82 @@ cudaError_t rfft_merge(int dtype, const void* in, void* z, const void* bcoef, in
                       static_cast<const float2*>(bcoef), h, batch, (float)s2);
   return pdl_launch(k_rfft_merge<double>, blocks, s, static_cast<const double2*>(in), static_cast<double2*>(z),
                     static_cast<const double2*>(bcoef), h, batch, s2);
+}
+
+namespace {
+unsigned blocks_for(long long items) { return (unsigned)((items + 255) / 256); }
+
+template <typename T>
+cudaError_t real_pre_t(int op, const void* in, void* z, const void* aux0, const void* aux1, int n, long long batch,
+                       double scale, double ortho, cudaStream_t s) {
+  using C = cx_t<T>;
+  switch (op) {
+    case kDct2: {
+      const int h = n / 2;
+      kern::DctPackLoad<T> ld{static_cast<const T*>(in), (long long)n, 0x7fffffff, n, (T)scale, (T)ortho};
+      return pdl_launch(k_pre<T, kern::DctPackLoad<T>>, blocks_for(batch * h), s, ld, static_cast<C*>(z), h, batch);
+    }
+    case kDct3: {
+      const int h = n / 2;
+      return pdl_launch(k_dct3_pre<T>, blocks_for(batch * ((n + 3) >> 2)), s, static_cast<const T*>(in),
+                        static_cast<C*>(z), static_cast<const C*>(aux0), static_cast<const C*>(aux1), h, batch,
+                        (T)scale, (T)ortho);
+    }
+    case kMdct: {
+      const int q = n / 4;
+      kern::MdctLoad<T> ld{static_cast<const T*>(in), (long long)n, 0x7fffffff, n, static_cast<const C*>(aux0),
+                           static_cast<const T*>(aux1)};
+      return pdl_launch(k_pre<T, kern::MdctLoad<T>>, blocks_for(batch * q), s, ld, static_cast<C*>(z), q, batch);
+    }
+    default: {  // kImdct
+      const int q = n / 4;
+      kern::ImdctLoad<T> ld{static_cast<const T*>(in), (long long)(n / 2), 0x7fffffff, n / 2,
+                            static_cast<const C*>(aux0)};
+      return pdl_launch(k_pre<T, kern::ImdctLoad<T>>, blocks_for(batch * q), s, ld, static_cast<C*>(z), q, batch);
+    }
+  }
+}
+
+template <typename T>
+cudaError_t real_post_t(int op, const void* z, void* out, const void* aux0, const void* aux1, int n, long long batch,
+                        double scale, cudaStream_t s) {
+  using C = cx_t<T>;
+  switch (op) {
+    case kDct2:
+      return pdl_launch(k_dct2_post<T>, blocks_for(batch * ((n + 3) >> 2)), s, static_cast<const C*>(z),
+                        static_cast<T*>(out), static_cast<const C*>(aux0), static_cast<const C*>(aux1), n / 2, batch);
+    case kDct3: {
+      kern::DctUnpackStore<T> st{static_cast<T*>(out), (long long)n, 0x7fffffff, n / 2};
+      // the backward core's output is conj(v) of the one-CTA kernel's v
+      return pdl_launch(k_post<T, kern::DctUnpackStore<T>>, blocks_for(batch * (n / 2)), s, st,
+                        static_cast<const C*>(z), n / 2, batch, 1);
+    }
+    case kMdct: {
+      kern::MdctStore<T> st{static_cast<T*>(out), (long long)(n / 2), 0x7fffffff, n / 2, static_cast<const C*>(aux0),
+                            (T)scale};
+      return pdl_launch(k_post<T, kern::MdctStore<T>>, blocks_for(batch * (n / 4)), s, st, static_cast<const C*>(z),
+                        n / 4, batch, 0);
+    }
+    default: {  // kImdct
+      kern::ImdctStore<T> st{static_cast<T*>(out), (long long)n, 0x7fffffff, n, static_cast<const C*>(aux0),
+                             static_cast<const T*>(aux1), (T)scale};
+      return pdl_launch(k_post<T, kern::ImdctStore<T>>, blocks_for(batch * (n / 4)), s, st, static_cast<const C*>(z),
+                        n / 4, batch, 0);
+    }
+  }
+}
+}  // namespace
+
+cudaError_t real_pre(int dtype, int op, const void* in, void* z, const void* aux0, const void* aux1, int n,
+                     long long batch, double scale, double ortho, cudaStream_t s) {
+  return dtype == 0 ? real_pre_t<float>(op, in, z, aux0, aux1, n, batch, scale, ortho, s)
+                    : real_pre_t<double>(op, in, z, aux0, aux1, n, batch, scale, ortho, s);
+}
+
+cudaError_t real_post(int dtype, int op, const void* z, void* out, const void* aux0, const void* aux1, int n,
+                      long long batch, double scale, cudaStream_t s) {
+  return dtype == 0 ? real_post_t<float>(op, z, out, aux0, aux1, n, batch, scale, s)
+                    : real_post_t<double>(op, z, out, aux0, aux1, n, batch, scale, s);
 }
 
 cudaError_t cluster_pass_tables(int dtype, int n, unsigned long long code, int np, void* out, cudaStream_t s) {

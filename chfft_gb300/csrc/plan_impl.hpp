@@ -196,6 +196,8 @@ struct PlanImpl {
         aux1.ensure((h + 1) * cb);
         gen(dct_type == CHFFT_DCT_TWO ? Table::RCOEF : Table::RBCOEF, len, h, aux0.p);
         gen(dct_type == CHFFT_DCT_TWO ? Table::OMEGA4N_POS : Table::OMEGA4N_NEG, len, h + 1, aux1.p);
+        clus.release();
+        if (!core.blue) clus.build(h, dtype, s);
         break;
       }
       case CHFFT_KIND_MDCT1D: {
@@ -208,6 +210,8 @@ struct PlanImpl {
           CHFFT_CUDA(cudaMemcpyAsync(aux1.p, custom_window.data(), len * rb, cudaMemcpyHostToDevice, s));
         else
           gen(window == CHFFT_WINDOW_VORBIS ? Table::VORBIS_WIN : Table::SINE_WIN, len, len, aux1.p);
+        clus.release();
+        if (!core.blue) clus.build(q, dtype, s);
         break;
       }
     }
@@ -433,6 +437,18 @@ struct PlanImpl {
         a.in_dist = a.out_dist = len;
         // ortho: x0 * sqrt(1/2) (DCT-II) or 1/2 -> sqrt(1/2) (DCT-III) (src/dct1d.rs:220-224, :343-347)
         a.aux_scalar = ortho ? std::sqrt(0.5) : (dct_type == CHFFT_DCT_TWO ? 1.0 : 0.5);
+        if (clus.n && batch <= clus.max_batch && opts.tc <= 0) {
+          // The half-length FFT on a cluster (scale 1, in place on the
+          // workspace) between the pre-twiddle / packing and the post launch;
+          // DCT-III's core runs backward on the unconjugated merge.
+          const int op = dct_type == CHFFT_DCT_TWO ? kDct2 : kDct3;
+          work.ensure((size_t)batch * (len / 2) * cplx_bytes(dtype));
+          CHFFT_CUDA(real_pre(dtype, op, d_in, work.p, aux0.p, aux1.p, (int)len, batch, sc, a.aux_scalar, s));
+          if (clus.exec(work.p, work.p, batch, op == kDct3, 1.0, s)) {
+            CHFFT_CUDA(real_post(dtype, op, work.p, d_out, aux0.p, aux1.p, (int)len, batch, sc, s));
+            return;
+          }
+        }
         launch<T>(dct_type == CHFFT_DCT_TWO ? Kernel::DCT2 : Kernel::DCT3, core, a, batch, s);
         return;
       case CHFFT_KIND_MDCT1D:
@@ -441,6 +457,17 @@ struct PlanImpl {
         a.n_user = (int)len;
         a.in_dist = ms.back ? len / 2 : len;
         a.out_dist = ms.back ? len : len / 2;
+        if (clus.n && batch <= clus.max_batch && opts.tc <= 0) {
+          // The quarter-length forward FFT on a cluster (in place on the
+          // workspace) between the fold / pre-twiddle and the post launch.
+          const int op = ms.back ? kImdct : kMdct;
+          work.ensure((size_t)batch * (len / 4) * cplx_bytes(dtype));
+          CHFFT_CUDA(real_pre(dtype, op, d_in, work.p, aux0.p, aux1.p, (int)len, batch, sc, 1.0, s));
+          if (clus.exec(work.p, work.p, batch, false, 1.0, s)) {
+            CHFFT_CUDA(real_post(dtype, op, work.p, d_out, aux0.p, aux1.p, (int)len, batch, sc, s));
+            return;
+          }
+        }
         launch<T>(ms.back ? Kernel::IMDCT : Kernel::MDCT, core, a, batch, s);
         return;
     }

@@ -211,3 +211,56 @@ def test_rfft1d_cluster_form_matches_oracle(dt, n):
         ref = np.stack([oracle.rfft1d(spec[i].astype(np.complex128), method) for i in range(3)])
         assert rel(z, ref) <= tol, method
     assert rel(p.execute_batch("backward", p.execute_batch("forward", xs)), xs) <= 2 * tol
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+@pytest.mark.parametrize("n", [128, 1024, 4096, 1152])
+@pytest.mark.parametrize("dct_type,ortho", [(2, False), (3, False), (2, True), (3, True)])
+def test_dct1d_cluster_form_matches_oracle(dt, n, dct_type, ortho):
+    """Dct1D runs its half-length FFT on a cluster at small batches (packing
+    and twiddles in launches of their own); every method matches the oracle
+    and the one-CTA plan (CHFFT_CLUSTER=0)."""
+    with env(CHFFT_CLUSTER=None):
+        p = cg.Dct1D(cg.DctType(dct_type), n, ortho, dt)
+    assert p.info().cluster_ctas in (8, 16)
+    with env(CHFFT_CLUSTER="0"):
+        q = cg.Dct1D(cg.DctType(dct_type), n, ortho, dt)
+    assert q.info().cluster_ctas == 0
+    rng = np.random.default_rng(n + dct_type)
+    xs = rng.uniform(-1, 1, (3, n)).astype(dt)
+    tol = TOL[dt]
+    for method in ("forward", "forwardu", "forwardn"):
+        y = p.execute_batch(method, xs)
+        ref = np.stack([oracle.dct1d(xs[i].astype(np.float64), dct_type, ortho, method) for i in range(3)])
+        assert rel(y, ref) <= tol, method
+        assert rel(y, q.execute_batch(method, xs)) <= tol, method
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+@pytest.mark.parametrize("n", [256, 1024, 4096, 2304])
+@pytest.mark.parametrize("window", ["sine", "vorbis"])
+def test_mdct1d_cluster_form_matches_oracle(dt, n, window):
+    """Mdct1D runs its quarter-length FFT on a cluster at small batches (fold,
+    window and twiddles in launches of their own), both directions, against
+    the oracle and the one-CTA plan."""
+    make = cg.Mdct1D.with_sine if window == "sine" else cg.Mdct1D.with_vorbis
+    with env(CHFFT_CLUSTER=None):
+        p = make(n, dt)
+    assert p.info().cluster_ctas in (8, 16)
+    with env(CHFFT_CLUSTER="0"):
+        q = make(n, dt)
+    assert q.info().cluster_ctas == 0
+    rng = np.random.default_rng(n)
+    xs = rng.uniform(-1, 1, (3, n)).astype(dt)
+    tol = TOL[dt]
+    for method in ("forward", "forwardu"):
+        y = p.execute_batch(method, xs)
+        ref = np.stack([oracle.mdct1d(xs[i].astype(np.float64), n, window, method) for i in range(3)])
+        assert rel(y, ref) <= tol, method
+        assert rel(y, q.execute_batch(method, xs)) <= tol, method
+    ys = rng.uniform(-1, 1, (3, n // 2)).astype(dt)
+    for method in ("backward", "backwardu"):
+        z = p.execute_batch(method, ys)
+        ref = np.stack([oracle.mdct1d(ys[i].astype(np.float64), n, window, method) for i in range(3)])
+        assert rel(z, ref) <= tol, method
+        assert rel(z, q.execute_batch(method, ys)) <= tol, method
