@@ -264,3 +264,42 @@ def test_mdct1d_cluster_form_matches_oracle(dt, n, window):
         ref = np.stack([oracle.mdct1d(ys[i].astype(np.float64), n, window, method) for i in range(3)])
         assert rel(z, ref) <= tol, method
         assert rel(z, q.execute_batch(method, ys)) <= tol, method
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+def test_real_kinds_cluster_form_in_place_device_and_graph(dt):
+    """Dct1D (II and III) and Mdct1D in the cluster form through
+    chfft_execute_device: in place (DCT), and replayed from a captured CUDA
+    graph, against the one-CTA plan's results."""
+    n, batch = 2048, 4
+    tdt = torch.float64 if dt == np.float64 else torch.float32
+    tol = TOL[dt]
+    rng = np.random.default_rng(11)
+    x = rng.uniform(-1, 1, (batch, n)).astype(dt)
+    for t in (2, 3):
+        with env(CHFFT_CLUSTER=None):
+            p = cg.Dct1D(cg.DctType(t), n, False, dt)
+        assert p.info().cluster_ctas in (8, 16)
+        with env(CHFFT_CLUSTER="0"):
+            ref = cg.Dct1D(cg.DctType(t), n, False, dt).execute_batch("forward", x)
+        d = torch.from_numpy(x).cuda()
+        s = torch.cuda.current_stream().cuda_stream
+        p.execute_device("forward", d.data_ptr(), d.data_ptr(), batch, s)  # in place
+        torch.cuda.synchronize()
+        assert rel(d.cpu().numpy(), ref) <= tol, t
+    with env(CHFFT_CLUSTER=None):
+        m = cg.Mdct1D.with_sine(n, dt)
+    assert m.info().cluster_ctas in (8, 16)
+    with env(CHFFT_CLUSTER="0"):
+        mref = cg.Mdct1D.with_sine(n, dt).execute_batch("forward", x)
+    d_in = torch.from_numpy(x).cuda()
+    d_out = torch.empty(batch, n // 2, dtype=tdt, device="cuda")
+    m.execute_device("forward", d_in.data_ptr(), d_out.data_ptr(), batch, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        m.execute_device("forward", d_in.data_ptr(), d_out.data_ptr(), batch, torch.cuda.current_stream().cuda_stream)
+    d_out.zero_()
+    g.replay()
+    torch.cuda.synchronize()
+    assert rel(d_out.cpu().numpy(), mref) <= tol
