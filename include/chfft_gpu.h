@@ -279,10 +279,12 @@ typedef struct chfft_plan_info {
   size_t smem_per_cta;
   size_t in_elems, out_elems; /* per transform, in the method's element type (forward direction) */
   size_t device_bytes;        /* tables + workspace held by the plan */
-  /* CFft1D latency form: batches of at most cluster_max_batch transforms run
-   * one transform per thread-block cluster of cluster_ctas CTAs (N =
-   * cluster_n1 x cluster_n2 split over the cluster, exchange through
-   * distributed shared memory); 0 when the plan has none. Plans of
+  /* Latency form: batches of at most cluster_max_batch transforms run the
+   * complex core (CFft1D: N; RFft1D and Dct1D: N/2; Mdct1D: N/4) one
+   * transform per thread-block cluster of cluster_ctas CTAs (the core split
+   * cluster_n1 x cluster_n2 over the cluster, exchange through distributed
+   * shared memory); the real kinds' pre- and post-processing run in
+   * launches of their own around it. 0 when the plan has none. Cores of
    * 7-smooth lengths from 64 to 2^20 with such a split that fits a CTA's
    * shared memory (CHFFT_CLUSTER=0 at plan creation turns it off, 8 or 16
    * forces the cluster size). */
