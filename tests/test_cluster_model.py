@@ -10,7 +10,9 @@ the cluster barrier each CTA runs the n2-point passes of its rows and
 stores X[k1 + n1 k2]. The model follows the kernel's index arithmetic
 (pass indexing, per-pass twiddle tables, per-CTA offsets, each CTA's
 table block) with numpy butterflies, and checks the shared-memory layout
-stays inside the launch's dynamic shared memory.
+stays inside the launch's dynamic shared memory. The real kinds' pre and
+post launches around the cluster core (k_cluster.cu real_pre / real_post)
+are restated too, with numpy's FFT as the core, against the oracle.
 """
 import numpy as np
 import pytest
@@ -226,3 +228,176 @@ def test_twiddle_part_product():
     w = complex(*rng.standard_normal(2))
     parts = [x.real * w.real + (-(x.imag * w.imag)), x.imag * w.real + (x.real * w.imag)]
     assert abs(complex(*parts) - x * w) < 1e-12
+
+
+# ---------------------------------------------------------------- real kinds
+# The cluster form of Dct1D / Mdct1D (k_cluster.cu real_pre / real_post):
+# a pre launch, the complex core on a cluster, a post launch. Restated here
+# with numpy's FFT standing in for the core, the plan tables as k_tables.cu
+# generates them, and checked against the oracle. DCT-III runs the core
+# backward (conj . F . conj) on the unconjugated merge, where the one-CTA
+# kernel runs it forward on the conjugated merge.
+
+def _root(p, q):
+    """exp(-2 pi i p / q)."""
+    return np.exp(-2j * np.pi * (np.asarray(p) % q) / q)
+
+
+def _tables_dct(n, dct_type):
+    h = n // 2
+    k = np.arange(h)
+    w = _root(k, n)                      # (c, s) = (cos, -sin)
+    c, s = w.real, w.imag
+    coef = (0.5 * (1 - s) + 0.5j * c) if dct_type == 2 else (0.5 * (1 - s) - 0.5j * c)
+    kk = np.arange(h + 1)
+    om = np.conj(_root(kk, 4 * n)) if dct_type == 2 else _root(kk, 4 * n)
+    return coef, om
+
+
+def _dct2_cluster(x, scale, ortho):
+    n = x.shape[-1]
+    h = n // 2
+    coef, om = _tables_dct(n, 2)
+
+    def v(j):  # DctPackLoad::v
+        return np.where(j < n // 2, x[np.minimum(2 * j, n - 1)], x[np.clip(2 * (n - 1 - j) + 1, 0, n - 1)])
+
+    m = np.arange(h)
+    re, im = v(2 * m), v(2 * m + 1)
+    re = np.where(m == 0, re * ortho, re)
+    z = np.fft.fft((re + 1j * im) * scale)   # the forward core
+    out = np.empty(n)
+    q2 = (n + 3) >> 2
+    z0 = z[0]
+    out[0] = z0.real + z0.imag
+    out[h] = (z0.real - z0.imag) * om[h].real
+    if n % 4 == 0:
+        xq = z[q2] * om[q2]
+        out[q2], out[n - q2] = xq.real, xq.imag
+    for i in range(1, q2):
+        zi, wc = z[i], np.conj(z[h - i])
+        xx = coef[i] * (zi - wc)
+        j = np.conj(zi - xx) * om[i]
+        out[i], out[n - i] = j.real, j.imag
+        kv = (wc + xx) * om[h - i]
+        out[h - i], out[h + i] = kv.real, kv.imag
+    return out
+
+
+def _dct3_cluster(x, scale, ortho):
+    n = x.shape[-1]
+    h = n // 2
+    coef, om = _tables_dct(n, 3)
+    q = (n + 3) >> 2
+    z = np.zeros(h, complex)
+    zval, hval = x[0] * ortho, x[h] * om[h].real
+    z[0] = (zval + hval) * scale + 1j * (zval - hval) * scale
+    if n % 4 == 0:
+        z[q] = (x[q] + 1j * x[n - q]) * om[q] * scale
+    for i in range(1, q):
+        j = np.conj((x[i] + 1j * x[n - i]) * om[i] * scale)
+        kv = (x[h - i] + 1j * x[h + i]) * om[h - i] * scale
+        xx = coef[i] * (j - kv)
+        z[i] = j - xx
+        z[h - i] = np.conj(kv + xx)
+    u = np.fft.ifft(z) * h                   # the backward core, scale 1
+    vv = np.conj(u)                          # k_post's conj_in: DctUnpackStore takes conj(u)
+    out = np.empty(n)
+    qh = h >> 1
+    for m in range(h):                       # DctUnpackStore::store(t, m, vv[m]) writes conj(vv[m])
+        re, im = vv[m].real, -vv[m].imag
+        if m < qh:
+            out[4 * m], out[4 * m + 2] = re, im
+        elif (h & 1) and m == qh:
+            out[2 * h - 2], out[2 * h - 1] = re, im
+        else:
+            i = h - 1 - m
+            out[4 * i + 1], out[4 * i + 3] = im, re
+    return out
+
+
+def _mdct_geom(n):
+    lenh = n >> 1
+    lenq = lenh >> 1
+    leno = lenq - (lenq >> 1)
+    return lenh, lenq, leno, lenh + lenq, lenh + lenh + lenq
+
+
+def _mdct_cluster(x, win, scale):
+    n = x.shape[-1]
+    q = n // 4
+    tw = _root(8 * np.arange(q) + 1, 8 * n) * (2.0 / n) ** 0.25
+    lenh, lenq, leno, len3q, len5q = _mdct_geom(n)
+    z = np.empty(q, complex)
+    for i in range(q):                       # MdctLoad
+        k = 2 * i
+        if i < leno:
+            re = x[len3q - 1 - k] * win[len3q - 1 - k] + x[len3q + k] * win[len3q + k]
+            im = x[lenq + k] * win[lenq + k] - x[lenq - 1 - k] * win[lenq - 1 - k]
+        else:
+            re = x[len3q - 1 - k] * win[len3q - 1 - k] - x[k - lenq] * win[k - lenq]
+            im = x[lenq + k] * win[lenq + k] + x[len5q - 1 - k] * win[len5q - 1 - k]
+        z[i] = (re + 1j * im) * tw[i]
+    y = np.fft.fft(z)                        # the forward core
+    out = np.empty(lenh)
+    for i in range(q):                       # MdctStore
+        r = y[i] * tw[i] * scale
+        out[2 * i], out[lenh - 1 - 2 * i] = -r.real, r.imag
+    return out
+
+
+def _imdct_cluster(s, n, win, scale):
+    q = n // 4
+    tw = _root(8 * np.arange(q) + 1, 8 * n) * (2.0 / n) ** 0.25
+    lenh, lenq, leno, len3q, len5q = _mdct_geom(n)
+    z = np.array([(s[2 * i] + 1j * s[lenh - 1 - 2 * i]) * tw[i] * -2.0 for i in range(q)])  # ImdctLoad
+    y = np.fft.fft(z)                        # the forward core
+    out = np.empty(n)
+    for i in range(q):                       # ImdctStore
+        k = 2 * i
+        r = y[i] * tw[i] * scale
+        if i < leno:
+            out[len3q - 1 - k] = r.real * win[len3q - 1 - k]
+            out[len3q + k] = r.real * win[len3q + k]
+            out[lenq + k] = -r.imag * win[lenq + k]
+            out[lenq - 1 - k] = r.imag * win[lenq - 1 - k]
+        else:
+            out[len3q - 1 - k] = r.real * win[len3q - 1 - k]
+            out[k - lenq] = -r.real * win[k - lenq]
+            out[lenq + k] = -r.imag * win[lenq + k]
+            out[len5q - 1 - k] = -r.imag * win[len5q - 1 - k]
+    return out
+
+
+@pytest.mark.parametrize("n", [16, 40, 128, 1152])
+@pytest.mark.parametrize("ortho", [False, True])
+def test_dct_cluster_form_model_matches_oracle(n, ortho):
+    import oracle
+    rng = np.random.default_rng(n)
+    x = rng.uniform(-1, 1, n)
+    for method, sc in (("forward", 1.0), ("forwardu", np.sqrt(2.0 / n)), ("forwardn", 2.0 / n)):
+        a2 = np.sqrt(0.5) if ortho else 1.0
+        y2 = _dct2_cluster(x, sc, a2)
+        r2 = oracle.dct1d(x, 2, ortho, method)
+        assert np.linalg.norm(y2 - r2) / np.linalg.norm(r2) < 1e-12, ("II", method)
+        a3 = np.sqrt(0.5) if ortho else 0.5
+        y3 = _dct3_cluster(x, sc, a3)
+        r3 = oracle.dct1d(x, 3, ortho, method)
+        assert np.linalg.norm(y3 - r3) / np.linalg.norm(r3) < 1e-12, ("III", method)
+
+
+@pytest.mark.parametrize("n", [16, 64, 2304])
+def test_mdct_cluster_form_model_matches_oracle(n):
+    import oracle
+    rng = np.random.default_rng(n)
+    x = rng.uniform(-1, 1, n)
+    win = np.sin(np.pi * (np.arange(n) + 0.5) / n)
+    for method, sc in (("forward", np.sqrt(n / 2.0)), ("forwardu", 1.0)):
+        y = _mdct_cluster(x, win, sc)
+        r = oracle.mdct1d(x, n, "sine", method)
+        assert np.linalg.norm(y - r) / np.linalg.norm(r) < 1e-12, method
+    s = rng.uniform(-1, 1, n // 2)
+    for method, sc in (("backward", 1.0 / np.sqrt(n / 2.0)), ("backwardu", 1.0)):
+        y = _imdct_cluster(s, n, win, sc)
+        r = oracle.mdct1d(s, n, "sine", method)
+        assert np.linalg.norm(y - r) / np.linalg.norm(r) < 1e-12, method
