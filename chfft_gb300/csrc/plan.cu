@@ -897,7 +897,8 @@ bool ClusterCore::build(long long n_, int dtype_, cudaStream_t s, bool beyond_ct
   // replay): f32 32768 at batches 1-4 32.8 against 36.8-38.9 us but 51
   // against 20 at batch 9, 65536 55 against 34.5; f64 16384 51 against 74
   // at batches 1-4, 96 against 74 at 9, 32768 even. So beyond one CTA the
-  // form takes f32 up to 32768 and f64 up to 16384, at most 4 transforms.
+  // form takes f32 up to 32768 (within the element bound below: 8
+  // transforms of 16384, 4 of 32768) and f64 up to 16384, at most 4.
   if (beyond_cta && !force && n_ > (dtype_ == 0 ? 32768 : 16384)) return false;
   const size_t cbytes = cplx_bytes(dtype_);
   struct Pick {
@@ -954,14 +955,19 @@ bool ClusterCore::build(long long n_, int dtype_, cudaStream_t s, bool beyond_ct
     code_a = best.ca;
     code_b = best.cb;
     smem = best.smem;
-    // Batches up to 2^18 (f64) or 2^16 (f32) elements, at most one
-    // transform per SM: measured crossovers against the one-CTA rows
-    // (GB300, forward + backward per graph replay): f64 4096 96 against
-    // 106 us at batch 76 but 174 against 106 at 152, 1024 43 against 55 at
-    // 152; f32 4096 20.5 against 20.4 at 38, 1024 14.3 against 14.3 at 76,
-    // 256 12.2 against 14.3 at 152 (CHFFT_CLUSTER_MAX_BATCH overrides).
-    max_batch = std::max<long long>(1, std::min<long long>(num_sms(), (dtype_ == 0 ? (1LL << 16) : (1LL << 18)) / n_));
-    if (beyond_cta) max_batch = std::min<long long>(max_batch, 4);
+    // Batches up to 2^18 (f64) or 2^16 (f32) elements, twice that from
+    // 8192 points up, at most one transform per SM: measured crossovers
+    // against the one-CTA rows (GB300, forward + backward per graph
+    // replay): f64 4096 96 against 106 us at batch 76 but 174 against 106
+    // at 152, 1024 43 against 55 at 152; f32 4096 20.5 against 20.4 at 38,
+    // 1024 14.3 against 14.3 at 76, 256 12.2 against 14.3 at 152. From 8192
+    // points the rows take the slower library kernel below 2^18 elements
+    // (forward: f32 8192 12.2 against 24.5 us at 16, 16384 18.4 against
+    // 32.7 at 8, f64 8192 88 against 108 at 64), so the cluster keeps the
+    // batches up to half that. CHFFT_CLUSTER_MAX_BATCH overrides.
+    const long long elems = (dtype_ == 0 ? (1LL << 16) : (1LL << 18)) << (n_ >= 8192 ? 1 : 0);
+    max_batch = std::max<long long>(1, std::min<long long>(num_sms(), elems / n_));
+    if (beyond_cta && dtype_ != 0) max_batch = std::min<long long>(max_batch, 4);
     if (const char* e = std::getenv("CHFFT_CLUSTER_MAX_BATCH")) max_batch = std::max(0LL, std::atoll(e));
     tab_a.ensure(std::max<size_t>(1, (size_t)(npa - 1) * n1) * cbytes);
     tab_b.ensure(std::max<size_t>(1, (size_t)(npb - 1) * n2) * cbytes);
