@@ -964,8 +964,11 @@ bool ClusterCore::build(long long n_, int dtype_, cudaStream_t s, bool beyond_ct
     // points the rows take the slower library kernel below 2^18 elements
     // (forward: f32 8192 12.2 against 24.5 us at 16, 16384 18.4 against
     // 32.7 at 8, f64 8192 88 against 108 at 64), so the cluster keeps the
-    // batches up to half that. CHFFT_CLUSTER_MAX_BATCH overrides.
-    const long long elems = (dtype_ == 0 ? (1LL << 16) : (1LL << 18)) << (n_ >= 8192 ? 1 : 0);
+    // batches up to half that; f32 within one CTA up to just below it
+    // (the cluster at 32 x 8192 takes 16.3 us, the library rows 24.5).
+    // CHFFT_CLUSTER_MAX_BATCH overrides.
+    long long elems = (dtype_ == 0 ? (1LL << 16) : (1LL << 18)) << (n_ >= 8192 ? 1 : 0);
+    if (dtype_ == 0 && !beyond_cta && n_ >= 8192) elems = (1LL << 18) - 1;  // want_specialised's bound
     max_batch = std::max<long long>(1, std::min<long long>(num_sms(), elems / n_));
     if (beyond_cta && dtype_ != 0) max_batch = std::min<long long>(max_batch, 4);
     if (const char* e = std::getenv("CHFFT_CLUSTER_MAX_BATCH")) max_batch = std::max(0LL, std::atoll(e));
