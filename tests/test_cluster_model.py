@@ -369,9 +369,13 @@ def _imdct_cluster(s, n, win, scale):
     return out
 
 
-@pytest.mark.parametrize("n", [16, 40, 128, 1152])
+@pytest.mark.parametrize("n", [16, 18, 40, 50, 128, 1152])
 @pytest.mark.parametrize("ortho", [False, True])
 def test_dct_cluster_form_model_matches_oracle(n, ortho):
+    """N = 2 mod 4 (18, 50) runs the odd-half branches of the pre / post
+    launches' formulas. The cluster path itself never takes them on the GPU
+    (its split makes the core a multiple of 64); the one-CTA kernels, whose
+    loops these restate, do."""
     import oracle
     rng = np.random.default_rng(n)
     x = rng.uniform(-1, 1, n)
