@@ -21,7 +21,8 @@ from the committed ncu summary.
 
 `--workload batch` is the other f32 configuration (4096 x N=1000, 4096 x
 N=1009 Chirp-Z, CFft2D 2048 x 2048); `uneven`, `costmodel` and `f64` the
-rest. `--impl reference` times the CPU oracle (a C++ restatement of chfft's
+rest; `latency` times the cluster form of small batches (RFft1D, Dct1D,
+Mdct1D, CFft1D) against the one-CTA plans. `--impl reference` times the CPU oracle (a C++ restatement of chfft's
 algorithm; the Rust crate cannot be built here) on a bounded sample of the
 same workload with every host thread.
 
@@ -999,6 +1000,139 @@ def run_costmodel(args):
     return 0
 
 
+def run_latency(args):
+    """Small batches in the cluster latency form against the one-CTA plans
+    (CHFFT_CLUSTER=0 at plan creation): CUDA-event time per CUDA-graph
+    replay of each case's launches, every forward result checked against
+    numpy / scipy in FP64 (f64 <= 1e-12, f32 <= 5e-6 relative L2; chfft's
+    DCT-II / DCT-III are half of scipy's types 2 / 3, its MDCT the
+    windowed definition)."""
+    import scipy.fft
+    import torch
+
+    import chfft_gb300 as cg
+
+    def mdct_def(x, n):
+        w = np.sin(np.pi * (np.arange(n) + 0.5) / n)
+        k, m = np.arange(n), np.arange(n // 2)
+        return (w * x) @ np.cos(np.pi / (2 * n) * np.outer(1 + n // 2 + 2 * k, 1 + 2 * m))
+
+    def plan_with(ctor, cluster):
+        old = os.environ.get("CHFFT_CLUSTER")
+        if cluster:
+            os.environ.pop("CHFFT_CLUSTER", None)
+        else:
+            os.environ["CHFFT_CLUSTER"] = "0"
+        try:
+            return ctor()
+        finally:
+            if old is None:
+                os.environ.pop("CHFFT_CLUSTER", None)
+            else:
+                os.environ["CHFFT_CLUSTER"] = old
+
+    # (name, kind, dtype, N, batch, methods run per replay, flops per transform and method)
+    cases = [
+        ("rfft1d_f64_1024_x1", "rfft1d", np.float64, 1024, 1, ("forward", "backward")),
+        ("rfft1d_f32_16384_x1", "rfft1d", np.float32, 16384, 1, ("forward", "backward")),
+        ("dct2_f64_16384_x1", "dct2", np.float64, 16384, 1, ("forward",)),
+        ("dct3_f64_1024_x8", "dct3", np.float64, 1024, 8, ("forward",)),
+        ("mdct_f64_1024_x1", "mdct1d", np.float64, 1024, 1, ("forward", "backward")),
+        ("mdct_f32_8192_x8", "mdct1d", np.float32, 8192, 8, ("forward",)),
+        ("cfft1d_f32_8192_x24", "cfft1d", np.float32, 8192, 24, ("forward",)),
+    ]
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    reps = max(args.steps, 100)
+    rows, tot_flops, tot_us, launches = {}, 0.0, 0.0, 0
+    for name, kind, dt, n, batch, methods in cases:
+        rdt = np.float64 if dt == np.float64 else np.float32
+        cdt = np.complex128 if dt == np.float64 else np.complex64
+        tdt = torch.float64 if dt == np.float64 else torch.float32
+        tol = 1e-12 if dt == np.float64 else 5e-6
+        rng = np.random.default_rng(n + batch)
+        if kind == "rfft1d":
+            ctor = lambda: cg.RFft1D(n, dt)  # noqa: E731
+            x = rng.uniform(-1, 1, (batch, n)).astype(rdt)
+            ref = np.fft.rfft(x.astype(np.float64), axis=-1)
+            flops = 2.5 * n * math.log2(n)
+        elif kind in ("dct2", "dct3"):
+            t = 2 if kind == "dct2" else 3
+            ctor = lambda: cg.Dct1D(cg.DctType(t), n, False, dt)  # noqa: E731
+            x = rng.uniform(-1, 1, (batch, n)).astype(rdt)
+            ref = scipy.fft.dct(x.astype(np.float64), type=t, axis=-1) / 2
+            flops = 2.5 * n * math.log2(n)
+        elif kind == "mdct1d":
+            ctor = lambda: cg.Mdct1D.with_sine(n, dt)  # noqa: E731
+            x = rng.uniform(-1, 1, (batch, n)).astype(rdt)
+            ref = np.stack([mdct_def(x[i].astype(np.float64), n) for i in range(batch)])
+            flops = 2.5 * n * math.log2(n)
+        else:
+            ctor = lambda: cg.CFft1D.with_len(n, dt)  # noqa: E731
+            x = (rng.uniform(-1, 1, (batch, n)) + 1j * rng.uniform(-1, 1, (batch, n))).astype(cdt)
+            ref = np.fft.fft(x.astype(np.complex128), axis=-1)
+            flops = 5.0 * n * math.log2(n)
+        res = {}
+        for form in ("cluster", "one_cta"):
+            p = plan_with(ctor, form == "cluster")
+            ctas = p.info().cluster_ctas
+            if form == "cluster" and (ctas == 0 or batch > p.info().cluster_max_batch):
+                raise SystemExit(f"{name}: the plan does not take the cluster form")
+            if form == "one_cta" and ctas != 0:
+                raise SystemExit(f"{name}: CHFFT_CLUSTER=0 left the cluster form on")
+            y = p.execute_batch("forward", x)
+            err = float(np.linalg.norm(np.asarray(y, np.complex128) - ref) / np.linalg.norm(ref))
+            if err > tol:
+                raise SystemExit(f"{name} ({form}): rel-L2 {err:.2e} against FP64 numpy / scipy > {tol}")
+            # device buffers: the forward output feeds the inverse
+            d_in = torch.from_numpy(np.ascontiguousarray(x).view(rdt)).to(dev)
+            d_mid = torch.from_numpy(np.ascontiguousarray(y).view(rdt)).to(dev)
+            d_out = torch.empty_like(d_in)
+
+            def issue(sp):
+                p.execute_device(methods[0], d_in.data_ptr(), d_mid.data_ptr(), batch, sp)
+                if len(methods) > 1:
+                    p.execute_device(methods[1], d_mid.data_ptr(), d_out.data_ptr(), batch, sp)
+
+            issue(stream.cuda_stream)
+            torch.cuda.synchronize()
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph):
+                issue(torch.cuda.current_stream().cuda_stream)
+            for _ in range(args.warmup):
+                graph.replay()
+            torch.cuda.synchronize()
+            evs = []
+            for _ in range(reps):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                graph.replay()
+                b.record(stream)
+                evs.append((a, b))
+            torch.cuda.synchronize()
+            res[form] = round(statistics.median(a.elapsed_time(b) for a, b in evs) * 1e3, 2)
+            res[form + "_rel_l2"] = err
+            if form == "cluster":
+                res["cluster_ctas"] = ctas
+                launches += reps * len(methods) * (1 if kind == "cfft1d" else 2 if kind == "rfft1d" else 3)
+        res["speedup"] = round(res["one_cta"] / res["cluster"], 2)
+        rows[name] = res
+        tot_flops += flops * batch * len(methods)
+        tot_us += res["cluster"]
+    line = {
+        "metric": METRIC, "value": round(tot_flops / (tot_us * 1e-6) / 1e9, 3), "unit": "GFLOP/s", "n_gpus": 1,
+        "steps": reps, "warmup": args.warmup, "ms_per_step": round(tot_us / 1e3, 5), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64/f32", "data": "synthetic uniform[-1,1), seeded",
+        "config": {"workload": "latency form: small batches of RFft1D, Dct1D, Mdct1D, CFft1D (cluster) against "
+                               "the one-CTA plans; value: all cases' flops over the sum of their cluster times",
+                   "l2": "resident (small batches)", "timing": "CUDA-event time per CUDA-graph replay, median"},
+        "latency_us": rows,
+        "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -1012,9 +1146,11 @@ def main():
                     help="uneven workload: time one class of its jobs (profiling)")
     ap.add_argument("--small", action="store_true",
                     help="default workload only: the same kernels at 2^20 x 16 and 4096 x 4096 (profiling case)")
-    ap.add_argument("--workload", choices=["precision", "batch", "uneven", "costmodel", "f64"], default="precision",
+    ap.add_argument("--workload", choices=["precision", "batch", "uneven", "costmodel", "f64", "latency"],
+                    default="precision",
                     help="precision: 64 x 2^20 + 16384 x 4096 with the tensor-core comparison (default); "
-                         "batch / uneven / costmodel / f64: the other configurations")
+                         "batch / uneven / costmodel / f64: the other configurations; latency: the cluster "
+                         "form of small batches against the one-CTA plans")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -1030,6 +1166,8 @@ def main():
         return run_costmodel(args)
     if args.workload == "f64":
         return run_f64(args)
+    if args.workload == "latency":
+        return run_latency(args)
     if world > 1:
         import torch
 
