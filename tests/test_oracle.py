@@ -246,3 +246,25 @@ def test_omega_table_symmetry():
         assert o.shape == (n + 1,)
         assert o[0] == 1 and o[n] == 1
         np.testing.assert_allclose(o[:n], np.exp(-2j * np.pi * np.arange(n) / n), atol=1e-15)
+
+
+@pytest.mark.parametrize("n", [16, 64, 1000, 2048])
+def test_bench_checkers_agree_with_the_oracle(n):
+    """bench.py checks its results against FP64 numpy / scipy (the oracle is
+    only timed there): chfft's DCT-II / DCT-III are half of scipy's types 2
+    / 3, and its MDCT is bench.mdct_def, the sine-windowed definition."""
+    import scipy.fft
+
+    import bench
+
+    rng = np.random.default_rng(n)
+    x = rng.uniform(-1, 1, n)
+    for t in (2, 3):
+        ref = oracle.dct1d(x, t, False, "forward")
+        got = scipy.fft.dct(x, type=t) / 2
+        assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-13, t
+    if n % 4 == 0:
+        ref = oracle.mdct1d(x, n, "sine", "forward")
+        assert np.linalg.norm(bench.mdct_def(x, n) - ref) / np.linalg.norm(ref) < 1e-12
+    z = x + 1j * rng.uniform(-1, 1, n)
+    assert np.linalg.norm(np.fft.ifft(np.fft.fft(z)) - oracle.cfft1d(oracle.cfft1d(z, "forward"), "backward")) < 1e-12
