@@ -405,3 +405,69 @@ def test_mdct_cluster_form_model_matches_oracle(n):
         y = _imdct_cluster(s, n, win, sc)
         r = oracle.mdct1d(s, n, "sine", method)
         assert np.linalg.norm(y - r) / np.linalg.norm(r) < 1e-12, method
+
+
+def _rfft_tables(n):
+    h = n // 2
+    w = _root(np.arange(h), n)
+    c, s = w.real, w.imag
+    return 0.5 * (1 - s) + 0.5j * c, 0.5 * (1 - s) - 0.5j * c   # RCOEF, RBCOEF
+
+
+def _rfft_split_model(x, scale):
+    """RFft1D forward in the cluster form: the half-length core on the
+    real input read as complex pairs, then k_rfft_split."""
+    n = x.shape[-1]
+    h = n // 2
+    coef, _ = _rfft_tables(n)
+    z = np.fft.fft(x[0::2] + 1j * x[1::2])   # the forward core, scale 1
+    q = (2 * h + 3) >> 2
+    o = np.empty(h + 1, complex)
+    o[0] = (z[0].real + z[0].imag) * scale
+    o[h] = (z[0].real - z[0].imag) * scale
+    if (2 * h) % 4 == 0:
+        o[q] = np.conj(z[q]) * scale
+    for i in range(1, q):
+        xx = coef[i] * (z[i] - np.conj(z[h - i]))
+        o[i] = (z[i] - xx) * scale
+        o[h - i] = (z[h - i] + np.conj(xx)) * scale
+    return o
+
+
+def _rfft_merge_model(spec, n, s2):
+    """RFft1D backward in the cluster form: k_rfft_merge (times 2 scale),
+    then the core backward (conj . F . conj, scale 1); the complex result
+    read as the N reals."""
+    h = n // 2
+    _, bcoef = _rfft_tables(n)
+    q = (2 * h + 3) >> 2
+    z = np.empty(h, complex)
+    z[0] = (spec[0].real + spec[h].real) * 0.5 * s2 + 1j * (spec[0].real - spec[h].real) * 0.5 * s2
+    if (2 * h) % 4 == 0:
+        z[q] = np.conj(spec[q]) * s2
+    for i in range(1, q):
+        xx = bcoef[i] * (spec[i] - np.conj(spec[h - i]))
+        z[i] = (spec[i] - xx) * s2
+        z[h - i] = (spec[h - i] + np.conj(xx)) * s2
+    u = np.fft.ifft(z) * h
+    out = np.empty(n)
+    out[0::2], out[1::2] = u.real, u.imag
+    return out
+
+
+@pytest.mark.parametrize("n", [16, 18, 128, 2304])
+def test_rfft_cluster_form_model_matches_oracle(n):
+    """The RFft1D cluster form's split (forward) and merge (backward) launches
+    around the half-length core reproduce the oracle for every method scale
+    (forward 1, 1/sqrt N, 1/N; backward 1/N, 1, 1/sqrt N; the merge takes
+    twice the method's scale)."""
+    import oracle
+    rng = np.random.default_rng(n)
+    x = rng.uniform(-1, 1, n)
+    for method, sc in (("forward", 1.0), ("forwardu", 1 / np.sqrt(n)), ("forwardn", 1.0 / n)):
+        ref = oracle.rfft1d(x, method)
+        assert np.linalg.norm(_rfft_split_model(x, sc) - ref) / np.linalg.norm(ref) < 1e-12, method
+    spec = np.fft.rfft(x)
+    for method, sc in (("backward", 1.0 / n), ("backward0", 1.0), ("backwardu", 1 / np.sqrt(n))):
+        ref = oracle.rfft1d(spec, method)
+        assert np.linalg.norm(_rfft_merge_model(spec, n, 2 * sc) - ref) / np.linalg.norm(ref) < 1e-12, method
