@@ -11,8 +11,9 @@ stores X[k1 + n1 k2]. The model follows the kernel's index arithmetic
 (pass indexing, per-pass twiddle tables, per-CTA offsets, each CTA's
 table block) with numpy butterflies, and checks the shared-memory layout
 stays inside the launch's dynamic shared memory. The real kinds' pre and
-post launches around the cluster core (k_cluster.cu real_pre / real_post)
-are restated too, with numpy's FFT as the core, against the oracle.
+post launches around the cluster core (k_cluster.cu k_rfft_split /
+k_rfft_merge, real_pre / real_post) are restated too, with numpy's FFT as
+the core, against the oracle.
 """
 import numpy as np
 import pytest
